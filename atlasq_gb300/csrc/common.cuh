@@ -1,0 +1,126 @@
+// Shared device helpers for the GB300 MPS kernels (sm_103a).
+// Complex values are interleaved (re, im): float2 for complex64, double2 for
+// complex128 -- the layout of torch.complex64 / torch.complex128 storage.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "atlasq_gb300.h"
+
+#define AGB_HD __host__ __device__ __forceinline__
+#define AGB_DEV __device__ __forceinline__
+
+template <typename CX> struct cx_traits;
+template <> struct cx_traits<float2> { typedef float R; };
+template <> struct cx_traits<double2> { typedef double R; };
+
+template <typename CX> AGB_HD CX mk(typename cx_traits<CX>::R re, typename cx_traits<CX>::R im) {
+  CX z;
+  z.x = re;
+  z.y = im;
+  return z;
+}
+template <typename CX> AGB_HD CX czero() { return mk<CX>(0, 0); }
+template <typename CX> AGB_HD CX cmul(CX a, CX b) { return mk<CX>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+// conj(a) * b
+template <typename CX> AGB_HD CX cmulc(CX a, CX b) { return mk<CX>(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x); }
+template <typename CX> AGB_HD CX cadd(CX a, CX b) { return mk<CX>(a.x + b.x, a.y + b.y); }
+template <typename CX> AGB_HD CX csub(CX a, CX b) { return mk<CX>(a.x - b.x, a.y - b.y); }
+template <typename CX> AGB_HD CX cconj(CX a) { return mk<CX>(a.x, -a.y); }
+template <typename CX> AGB_HD CX cscale(CX a, typename cx_traits<CX>::R s) { return mk<CX>(a.x * s, a.y * s); }
+template <typename CX> AGB_HD typename cx_traits<CX>::R cabs2(CX a) { return a.x * a.x + a.y * a.y; }
+// 1 / z
+template <typename CX> AGB_HD CX cinv(CX z) {
+  typename cx_traits<CX>::R d = z.x * z.x + z.y * z.y;
+  return mk<CX>(z.x / d, -z.y / d);
+}
+// acc += a * b
+template <typename CX> AGB_HD void cfma(CX& acc, CX a, CX b) {
+  acc.x = fma(a.x, b.x, acc.x);
+  acc.x = fma(-a.y, b.y, acc.x);
+  acc.y = fma(a.x, b.y, acc.y);
+  acc.y = fma(a.y, b.x, acc.y);
+}
+// acc += conj(a) * b
+template <typename CX> AGB_HD void cfmac(CX& acc, CX a, CX b) {
+  acc.x = fma(a.x, b.x, acc.x);
+  acc.x = fma(a.y, b.y, acc.x);
+  acc.y = fma(a.x, b.y, acc.y);
+  acc.y = fma(-a.y, b.x, acc.y);
+}
+
+template <typename T> AGB_DEV T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+template <typename CX> AGB_DEV CX warp_csum(CX v) {
+  v.x = warp_sum(v.x);
+  v.y = warp_sum(v.y);
+  return v;
+}
+
+// Block-wide sum of one value per thread; `red` must hold >= 32 entries.
+// All threads of the block must call it; every thread gets the result.
+template <typename T> AGB_DEV T block_sum(T v, T* red) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  T t = (threadIdx.x < nw) ? red[threadIdx.x] : T(0);
+  if (wid == 0) t = warp_sum(t);
+  if (threadIdx.x == 0) red[0] = t;
+  __syncthreads();
+  T r = red[0];
+  __syncthreads();
+  return r;
+}
+
+// ---------------------------------------------------------------- Philox4x32-10
+// Salmon, Moraes, Dror, Shaw, SC'11 (Random123).  Same definition as the CPU
+// oracle: ten rounds, multipliers 0xD2511F53 / 0xCD9E8D57, Weyl increments
+// 0x9E3779B9 / 0xBB67AE85.
+struct philox_out {
+  uint32_t x, y, z, w;
+};
+AGB_DEV philox_out philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0,
+                                  uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    if (r > 0) {
+      k0 += 0x9E3779B9u;
+      k1 += 0xBB67AE85u;
+    }
+    const uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
+    const uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
+    const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+    c0 = n0;
+    c1 = lo1;
+    c2 = n2;
+    c3 = lo0;
+  }
+  philox_out o;
+  o.x = c0;
+  o.y = c1;
+  o.z = c2;
+  o.w = c3;
+  return o;
+}
+
+// Standard normal from Philox words (Box-Muller on 24-bit uniforms).
+AGB_DEV float philox_normal(uint64_t seed, uint64_t idx, uint32_t stream) {
+  philox_out o = philox4x32_10((uint32_t)idx, (uint32_t)(idx >> 32), stream, 0x5EEDu, (uint32_t)seed,
+                               (uint32_t)(seed >> 32));
+  const float u1 = ((float)(o.x >> 8) + 1.0f) * (1.0f / 16777216.0f);
+  const float u2 = (float)(o.y >> 8) * (1.0f / 16777216.0f);
+  return sqrtf(-2.0f * logf(u1)) * cospif(2.0f * u2);
+}
+
+AGB_HD size_t agb_align(size_t x) { return (x + 255) & ~(size_t)255; }
+
+#define AGB_CHECK_LAUNCH()                      \
+  do {                                          \
+    cudaError_t _e = cudaGetLastError();        \
+    if (_e != cudaSuccess) return AGB_ERR_CUDA; \
+  } while (0)

@@ -1,0 +1,598 @@
+// Batched Hermitian eigensolver kernels (see heevd.cuh for the stage list).
+#include <float.h>
+
+#include "heevd.cuh"
+
+template <typename R> struct rlim;
+template <> struct rlim<float> {
+  static AGB_HD float eps() { return FLT_EPSILON; }
+  static AGB_HD float pivmin() { return 1e-30f; }
+};
+template <> struct rlim<double> {
+  static AGB_HD double eps() { return DBL_EPSILON; }
+  static AGB_HD double pivmin() { return 1e-290; }
+};
+
+void heevd_assign_scratch(HeevdProb& p, char* base, int esz) { heevd_assign_scratch_dev(p, base, esz); }
+
+namespace {
+
+// ------------------------------------------------------------------ stage 1
+// Householder reflector for step j (zlarfg semantics): x = column j below the
+// diagonal = conj(row j, cols > j).  Writes v into smem (v[j+1] = 1) and into
+// row j of H (cols >= j+2); returns tau, beta via smem broadcast.
+template <typename CX>
+AGB_DEV void make_reflector(CX* H, int64_t ld, int n, int j, CX* v, typename cx_traits<CX>::R* red,
+                            CX* bc, typename cx_traits<CX>::R* d, typename cx_traits<CX>::R* e,
+                            CX* tau) {
+  typedef typename cx_traits<CX>::R R;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  CX* row = H + (int64_t)j * ld;
+  R part = 0;
+  for (int c = j + 2 + tid; c < n; c += nt) part += cabs2(row[c]);
+  const R xnorm2 = block_sum(part, red);
+  if (tid == 0) {
+    const CX alpha = cconj(row[j + 1]);
+    CX t = czero<CX>(), sc = czero<CX>();
+    R beta;
+    if (xnorm2 == R(0) && alpha.y == R(0)) {
+      beta = alpha.x;
+    } else {
+      beta = -copysign(sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xnorm2), alpha.x);
+      t = mk<CX>((beta - alpha.x) / beta, -alpha.y / beta);
+      sc = cinv(csub(alpha, mk<CX>(beta, 0)));
+    }
+    bc[0] = t;
+    bc[1] = sc;
+    e[j] = beta;
+    tau[j] = t;
+    d[j] = row[j].x;
+  }
+  __syncthreads();
+  const CX sc = bc[1];
+  for (int c = j + 2 + tid; c < n; c += nt) {
+    const CX vc = cmul(cconj(row[c]), sc);
+    v[c] = vc;
+    row[c] = vc;
+  }
+  if (tid == 0) v[j + 1] = mk<CX>(1, 0);
+  __syncthreads();
+}
+
+template <typename CX>
+__global__ void __launch_bounds__(1024) tridiag_kernel(const HeevdProb* __restrict__ probs) {
+  typedef typename cx_traits<CX>::R R;
+  const HeevdProb P = probs[blockIdx.x];
+  const int n = P.n;
+  if (n <= 0) return;
+  CX* H = (CX*)P.H;
+  const int64_t ld = P.ldh;
+  R* d = (R*)P.d;
+  R* e = (R*)P.e;
+  CX* tau = (CX*)P.tau;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  CX* va = (CX*)smem_raw;
+  CX* vb = va + n;
+  CX* w = vb + n;
+  CX* pv = w + n;
+  __shared__ R red[32];
+  __shared__ CX bc[4];
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, wid = tid >> 5, nw = nt >> 5;
+
+  // scale by the largest diagonal magnitude (Gram matrices: largest column norm)
+  R mx = 0;
+  for (int i = tid; i < n; i += nt) mx = fmax(mx, fabs(H[(int64_t)i * ld + i].x));
+  {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (lane == 0) red[wid] = mx;
+    __syncthreads();
+    if (tid == 0) {
+      R m = 0;
+      for (int i = 0; i < nw; ++i) m = fmax(m, red[i]);
+      red[0] = m;
+    }
+    __syncthreads();
+    mx = red[0];
+    __syncthreads();
+  }
+  if (mx == R(0)) mx = R(1);
+  if (tid == 0) *((R*)P.scale) = mx;
+  const R inv = R(1) / mx;
+  for (int64_t idx = tid; idx < (int64_t)n * n; idx += nt) {
+    const int r = (int)(idx / n), c = (int)(idx % n);
+    CX* a = H + (int64_t)r * ld + c;
+    *a = cscale(*a, inv);
+  }
+  __syncthreads();
+  if (n == 1) {
+    if (tid == 0) {
+      d[0] = H[0].x;
+      e[0] = 0;
+      tau[0] = czero<CX>();
+    }
+    return;
+  }
+  CX* v = va;
+  CX* vn = vb;
+  // reflector 0 and its matvec p = tau * H[1:,1:] v
+  make_reflector(H, ld, n, 0, v, red, bc, d, e, tau);
+  {
+    const CX t0 = tau[0];
+    for (int r = 1 + wid; r < n; r += nw) {
+      const CX* row = H + (int64_t)r * ld;
+      CX acc = czero<CX>();
+      for (int c = 1 + lane; c < n; c += 32) cfma(acc, row[c], v[c]);
+      acc = warp_csum(acc);
+      if (lane == 0) pv[r] = cmul(t0, acc);
+    }
+  }
+  __syncthreads();
+  for (int j = 0; j <= n - 2; ++j) {
+    const CX t = tau[j];
+    const bool active = (t.x != R(0) || t.y != R(0));
+    if (active) {
+      // K = -1/2 tau (p^H v); w = p + K v   over r >= j+1
+      CX part = czero<CX>();
+      for (int r = j + 1 + tid; r < n; r += nt) cfmac(part, pv[r], v[r]);
+      const R sr = block_sum(part.x, red);
+      const R si = block_sum(part.y, red);
+      const CX K = cscale(cmul(t, mk<CX>(sr, si)), R(-0.5));
+      for (int r = j + 1 + tid; r < n; r += nt) w[r] = cadd(pv[r], cmul(K, v[r]));
+      __syncthreads();
+      // row j+1, cols >= j+1:  H -= v w^H + w v^H   (v[j+1] = 1)
+      CX* row = H + (int64_t)(j + 1) * ld;
+      const CX wr = w[j + 1];
+      for (int c = j + 1 + tid; c < n; c += nt) {
+        CX a = row[c];
+        a = csub(a, cconj(w[c]));          // v[j+1] * conj(w[c])
+        a = csub(a, cmul(wr, cconj(v[c])));
+        row[c] = a;
+      }
+      __syncthreads();
+    }
+    CX tn = czero<CX>();
+    if (j + 1 <= n - 2) {
+      make_reflector(H, ld, n, j + 1, vn, red, bc, d, e, tau);
+      tn = tau[j + 1];
+    } else {
+      if (tid == 0) {
+        d[n - 1] = H[(int64_t)(n - 1) * ld + (n - 1)].x;
+        e[n - 1] = 0;
+      }
+    }
+    const bool next_active = (tn.x != R(0) || tn.y != R(0));
+    // fused pass over rows r >= j+2: apply step-j update, accumulate next matvec
+    if (active || next_active) {
+      for (int r = j + 2 + wid; r < n; r += nw) {
+        CX* row = H + (int64_t)r * ld;
+        const CX vr = v[r], wr = w[r];
+        CX acc = czero<CX>();
+        for (int c = j + 2 + lane; c < n; c += 32) {
+          CX a = row[c];
+          if (active) {
+            a = csub(a, cmul(vr, cconj(w[c])));
+            a = csub(a, cmul(wr, cconj(v[c])));
+            row[c] = a;
+          }
+          if (next_active) cfma(acc, a, vn[c]);
+        }
+        if (next_active) {
+          acc = warp_csum(acc);
+          if (lane == 0) pv[r] = cmul(tn, acc);
+        }
+      }
+    }
+    __syncthreads();
+    CX* tmp = v;
+    v = vn;
+    vn = tmp;
+  }
+}
+
+// ------------------------------------------------------------------ stage 2
+template <typename R>
+AGB_DEV int sturm_count(const R* d, const R* e2, int n, R x) {
+  const R pm = rlim<R>::pivmin();
+  R q = d[0] - x;
+  int cnt = q < R(0);
+  for (int i = 1; i < n; ++i) {
+    if (fabs(q) < pm) q = -pm;
+    q = d[i] - x - e2[i - 1] / q;
+    cnt += q < R(0);
+  }
+  return cnt;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) bisect_kernel(const HeevdProb* __restrict__ probs) {
+  const HeevdProb P = probs[blockIdx.y];
+  const int n = P.n, ell = P.ell;
+  if (blockIdx.x * 8 >= ell) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  R* d = (R*)smem_raw;
+  R* e2 = d + n;
+  __shared__ R glim[2];
+  const R* dg = (const R*)P.d;
+  const R* eg = (const R*)P.e;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    d[i] = dg[i];
+    e2[i] = (i < n - 1) ? eg[i] * eg[i] : R(0);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    R gl = d[0], gu = d[0];
+    for (int i = 0; i < n; ++i) {
+      const R r = (i > 0 ? fabs(eg[i - 1]) : R(0)) + (i < n - 1 ? fabs(eg[i]) : R(0));
+      gl = fmin(gl, d[i] - r);
+      gu = fmax(gu, d[i] + r);
+    }
+    const R span = fmax(fabs(gl), fabs(gu));
+    glim[0] = gl - R(4) * rlim<R>::eps() * span - rlim<R>::pivmin();
+    glim[1] = gu + R(4) * rlim<R>::eps() * span + rlim<R>::pivmin();
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int t = blockIdx.x * 8 + wid;
+  if (t >= ell) return;
+  const int idx = n - 1 - t;  // ascending index of the t-th largest eigenvalue
+  R lo = glim[0], hi = glim[1];
+  const R tol = R(2) * rlim<R>::eps() * fmax(fabs(lo), fabs(hi));
+  for (int it = 0; it < 64 && hi - lo > tol; ++it) {
+    const R x = lo + (hi - lo) * R(lane + 1) / R(33);
+    const int c = sturm_count(d, e2, n, x);
+    const unsigned m = __ballot_sync(0xffffffffu, c > idx);
+    const int f = m ? __ffs(m) - 1 : 32;
+    const R nhi = (f < 32) ? __shfl_sync(0xffffffffu, x, f) : hi;
+    const R nlo = (f > 0) ? __shfl_sync(0xffffffffu, x, (f > 0 ? f - 1 : 0)) : lo;
+    if (nhi == hi && nlo == lo) break;
+    lo = nlo;
+    hi = nhi;
+  }
+  if (lane == 0) ((R*)P.lam)[t] = R(0.5) * (lo + hi);
+}
+
+// ------------------------------------------------------------------ stage 3
+template <typename R>
+__global__ void __launch_bounds__(128) invit_kernel(const HeevdProb* __restrict__ probs) {
+  const HeevdProb P = probs[blockIdx.y];
+  const int n = P.n, ell = P.ell;
+  if (blockIdx.x * 128 >= ell) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  R* d = (R*)smem_raw;
+  R* e = d + n;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    d[i] = ((const R*)P.d)[i];
+    e[i] = (i < n - 1) ? ((const R*)P.e)[i] : R(0);
+  }
+  __syncthreads();
+  const int t = blockIdx.x * 128 + threadIdx.x;
+  if (t >= ell) return;
+  const R lam = ((const R*)P.lam)[t];
+  R tnorm = 0;
+  for (int i = 0; i < n; ++i) tnorm = fmax(tnorm, fabs(d[i]) + fabs(e[i]) + (i ? fabs(e[i - 1]) : R(0)));
+  const R piv = rlim<R>::eps() * fmax(tnorm, rlim<R>::pivmin());
+  R* lu = (R*)P.lu;
+  const int64_t L = ell;
+  R* U0 = lu;
+  R* U1 = lu + (int64_t)n * L;
+  R* U2 = lu + 2 * (int64_t)n * L;
+  R* Lm = lu + 3 * (int64_t)n * L;
+  R* Pv = lu + 4 * (int64_t)n * L;
+  // LU with partial pivoting of T - lam I (rows carry up to two superdiagonals)
+  R u0 = d[0] - lam, u1 = (n > 1) ? e[0] : R(0), u2 = 0;
+  for (int i = 0; i < n - 1; ++i) {
+    const R sub = e[i], nd = d[i + 1] - lam, ns = (i + 1 < n - 1) ? e[i + 1] : R(0);
+    R a0, a1, a2, m, pv;
+    if (fabs(u0) >= fabs(sub)) {
+      if (u0 == R(0)) u0 = piv;
+      m = sub / u0;
+      a0 = u0; a1 = u1; a2 = u2;
+      u0 = nd - m * u1;
+      u1 = ns - m * u2;
+      pv = 0;
+    } else {
+      m = u0 / sub;
+      a0 = sub; a1 = nd; a2 = ns;
+      const R nu0 = u1 - m * nd, nu1 = u2 - m * ns;
+      u0 = nu0;
+      u1 = nu1;
+      pv = 1;
+    }
+    u2 = 0;
+    U0[i * L + t] = a0;
+    U1[i * L + t] = a1;
+    U2[i * L + t] = a2;
+    Lm[i * L + t] = m;
+    Pv[i * L + t] = pv;
+  }
+  if (fabs(u0) < piv) u0 = copysign(piv, u0 == R(0) ? R(1) : u0);
+  U0[(int64_t)(n - 1) * L + t] = u0;
+  U1[(int64_t)(n - 1) * L + t] = 0;
+  U2[(int64_t)(n - 1) * L + t] = 0;
+  R* Y = (R*)P.Y;
+  // random start
+  R nrm = 0;
+  for (int i = 0; i < n; ++i) {
+    const R b = (R)philox_normal(P.seed, (uint64_t)t * (uint64_t)n + i, 0x11u);
+    Y[i * L + t] = b;
+    nrm += b * b;
+  }
+  for (int it = 0; it < 3; ++it) {
+    const R s = R(1) / sqrt(fmax(nrm, rlim<R>::pivmin()));
+    // forward: apply P and L
+    R bi = Y[t] * s;
+    for (int i = 0; i < n - 1; ++i) {
+      R bn = Y[(i + 1) * L + t] * s;
+      if (Pv[i * L + t] != R(0)) {
+        const R tmp = bi;
+        bi = bn;
+        bn = tmp;
+      }
+      Y[i * L + t] = bi;
+      bi = bn - Lm[i * L + t] * bi;
+    }
+    Y[(int64_t)(n - 1) * L + t] = bi;
+    // backward substitution
+    R x1 = 0, x2 = 0;
+    nrm = 0;
+    for (int i = n - 1; i >= 0; --i) {
+      R u = U0[i * L + t];
+      if (fabs(u) < piv) u = copysign(piv, u == R(0) ? R(1) : u);
+      const R x = (Y[i * L + t] - U1[i * L + t] * x1 - U2[i * L + t] * x2) / u;
+      Y[i * L + t] = x;
+      nrm += x * x;
+      x2 = x1;
+      x1 = x;
+    }
+    if (!(nrm < R(1e300)) || !(nrm > R(0))) {  // overflow / breakdown: restart from a unit vector
+      for (int i = 0; i < n; ++i) Y[i * L + t] = (i == (t % n)) ? R(1) : R(0);
+      nrm = 1;
+    }
+  }
+  const R s = R(1) / sqrt(fmax(nrm, rlim<R>::pivmin()));
+  for (int i = 0; i < n; ++i) Y[i * L + t] *= s;
+}
+
+// ------------------------------------------------------------------ stage 4
+template <typename R>
+__global__ void __launch_bounds__(256) cluster_mgs_kernel(const HeevdProb* __restrict__ probs, double tolrel) {
+  const HeevdProb P = probs[blockIdx.x];
+  const int n = P.n, ell = P.ell;
+  if (ell < 2) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  int* start = (int*)smem_raw;  // cluster start for each index
+  const R* lam = (const R*)P.lam;
+  if (threadIdx.x == 0) {
+    const R scale = fmax(fabs(lam[0]), fabs(lam[ell - 1]));
+    const R tol = (R)tolrel * fmax(scale, rlim<R>::pivmin());
+    int s = 0;
+    for (int t = 0; t < ell; ++t) {
+      if (t > 0 && (lam[t - 1] - lam[t]) > tol) s = t;
+      start[t] = s;
+    }
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  R* Y = (R*)P.Y;
+  const int64_t L = ell;
+  // a warp owns a cluster if it owns the cluster's first index (round robin by start)
+  int cid = 0;
+  for (int t = 0; t < ell; ++t) {
+    if (start[t] != t) continue;
+    int end = t + 1;
+    while (end < ell && start[end] == t) ++end;
+    const bool mine = (cid % nw) == wid;
+    ++cid;
+    if (!mine || end - t < 2) continue;
+    for (int pass = 0; pass < 2; ++pass) {
+      for (int j = t; j < end; ++j) {
+        for (int i = t; i < j; ++i) {
+          R dot = 0;
+          for (int r = lane; r < n; r += 32) dot += Y[r * L + i] * Y[r * L + j];
+          dot = warp_sum(dot);
+          for (int r = lane; r < n; r += 32) Y[r * L + j] -= dot * Y[r * L + i];
+          __syncwarp();
+        }
+        R nrm = 0;
+        for (int r = lane; r < n; r += 32) nrm += Y[r * L + j] * Y[r * L + j];
+        nrm = warp_sum(nrm);
+        const R s = R(1) / sqrt(fmax(nrm, rlim<R>::pivmin()));
+        for (int r = lane; r < n; r += 32) Y[r * L + j] *= s;
+        __syncwarp();
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------ stage 5
+template <typename CX, int NK>
+__global__ void __launch_bounds__(256) backtransform_kernel(const HeevdProb* __restrict__ probs) {
+  typedef typename cx_traits<CX>::R R;
+  const HeevdProb P = probs[blockIdx.y];
+  const int n = P.n, ell = P.ell;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int t = blockIdx.x * 8 + wid;
+  if (t >= ell || n > NK * 32) return;
+  const R* Y = (const R*)P.Y;
+  CX z[NK];
+#pragma unroll
+  for (int k = 0; k < NK; ++k) {
+    const int r = lane + 32 * k;
+    z[k] = (r < n) ? mk<CX>(Y[(int64_t)r * ell + t], 0) : czero<CX>();
+  }
+  const CX* H = (const CX*)P.H;
+  const CX* tau = (const CX*)P.tau;
+  for (int j = n - 2; j >= 0; --j) {
+    const CX tj = tau[j];
+    if (tj.x == R(0) && tj.y == R(0)) continue;
+    const CX* row = H + (int64_t)j * P.ldh;
+    CX s = czero<CX>();
+#pragma unroll
+    for (int k = 0; k < NK; ++k) {
+      const int r = lane + 32 * k;
+      if (r >= j + 1 && r < n) {
+        const CX vr = (r == j + 1) ? mk<CX>(1, 0) : row[r];
+        cfmac(s, vr, z[k]);
+      }
+    }
+    s = warp_csum(s);
+    const CX ts = cmul(tj, s);
+#pragma unroll
+    for (int k = 0; k < NK; ++k) {
+      const int r = lane + 32 * k;
+      if (r >= j + 1 && r < n) {
+        const CX vr = (r == j + 1) ? mk<CX>(1, 0) : row[r];
+        z[k] = csub(z[k], cmul(vr, ts));
+      }
+    }
+  }
+  CX* V = (CX*)P.V;
+#pragma unroll
+  for (int k = 0; k < NK; ++k) {
+    const int r = lane + 32 * k;
+    if (r < n) V[(int64_t)r * P.ldv + t] = z[k];
+  }
+}
+
+// ------------------------------------------------------------------ stage 6
+// GEMM problems for one Newton-Schulz step: M = Vs^H Vs; Vd = 1.5 Vs - 0.5 Vs M
+__global__ void polish_setup_kernel(const HeevdProb* __restrict__ probs, GemmProb* gp, int count,
+                                    int step) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const HeevdProb P = probs[i];
+  const bool fwd = (step == 0);
+  const void* Vs = fwd ? P.V : P.V2;
+  void* Vd = fwd ? P.V2 : P.V;
+  const int64_t lds = fwd ? P.ldv : P.ell;
+  const int64_t ldd = fwd ? P.ell : P.ldv;
+  GemmProb g;
+  g.A = Vs; g.B = Vs; g.D = P.M; g.Csrc = P.M;
+  g.lda = lds; g.ldb = lds; g.ldd = P.ell; g.ldc = P.ell;
+  g.M = P.ell; g.N = P.ell; g.K = P.n;
+  g.opA = 2; g.opB = 0;
+  g.alpha_re = 1; g.alpha_im = 0; g.beta_re = 0; g.beta_im = 0;
+  gp[i] = g;
+  GemmProb h;
+  h.A = Vs; h.B = P.M; h.D = Vd; h.Csrc = Vs;
+  h.lda = lds; h.ldb = P.ell; h.ldd = ldd; h.ldc = lds;
+  h.M = P.n; h.N = P.ell; h.K = P.ell;
+  h.opA = 0; h.opB = 0;
+  h.alpha_re = -0.5; h.alpha_im = 0; h.beta_re = 1.5; h.beta_im = 0;
+  gp[count + i] = h;
+}
+
+template <typename CX, int NK>
+int launch_bt(const HeevdProb* probs, int count, int maxell, cudaStream_t s) {
+  dim3 grid((maxell + 7) / 8, count);
+  backtransform_kernel<CX, NK><<<grid, 256, 0, s>>>(probs);
+  AGB_CHECK_LAUNCH();
+  return AGB_OK;
+}
+
+}  // namespace
+
+template <typename CX>
+int launch_heevd(HeevdProb* probs, GemmProb* gp, int count, int maxn, int maxell, cudaStream_t s) {
+  typedef typename cx_traits<CX>::R R;
+  if (count <= 0 || maxn <= 0) return AGB_OK;
+  if (maxn > 1024) return AGB_ERR_UNSUPPORTED;
+  const int esz = sizeof(CX);
+  const size_t sm_tri = 4 * (size_t)maxn * esz;
+  static bool attr_set[2] = {false, false};
+  if (!attr_set[esz == 16]) {
+    cudaFuncSetAttribute(tridiag_kernel<CX>, cudaFuncAttributeMaxDynamicSharedMemorySize, 65536);
+    attr_set[esz == 16] = true;
+  }
+  tridiag_kernel<CX><<<count, 1024, sm_tri, s>>>(probs);
+  AGB_CHECK_LAUNCH();
+  if (maxell <= 0) return AGB_OK;
+  const size_t sm_r = 2 * (size_t)maxn * sizeof(R);
+  bisect_kernel<R><<<dim3((maxell + 7) / 8, count), 256, sm_r, s>>>(probs);
+  AGB_CHECK_LAUNCH();
+  invit_kernel<R><<<dim3((maxell + 127) / 128, count), 128, sm_r, s>>>(probs);
+  AGB_CHECK_LAUNCH();
+  cluster_mgs_kernel<R><<<count, 256, (size_t)maxell * sizeof(int), s>>>(probs, 1e-4);
+  AGB_CHECK_LAUNCH();
+  int rc;
+  if (maxn <= 128) rc = launch_bt<CX, 4>(probs, count, maxell, s);
+  else if (maxn <= 256) rc = launch_bt<CX, 8>(probs, count, maxell, s);
+  else if (maxn <= 512) rc = launch_bt<CX, 16>(probs, count, maxell, s);
+  else rc = launch_bt<CX, 32>(probs, count, maxell, s);
+  if (rc) return rc;
+  for (int step = 0; step < 2; ++step) {
+    polish_setup_kernel<<<(count + 127) / 128, 128, 0, s>>>(probs, gp, count, step);
+    AGB_CHECK_LAUNCH();
+    if ((rc = launch_gemm_probs<CX>(gp, count, maxell, maxell, s))) return rc;
+    if ((rc = launch_gemm_probs<CX>(gp + count, count, maxn, maxell, s))) return rc;
+  }
+  return AGB_OK;
+}
+
+template int launch_heevd<float2>(HeevdProb*, GemmProb*, int, int, int, cudaStream_t);
+template int launch_heevd<double2>(HeevdProb*, GemmProb*, int, int, int, cudaStream_t);
+
+// ------------------------------------------------------------------ standalone entry
+namespace {
+__global__ void heevd_setup_kernel(HeevdProb* probs, void* H, void* evecs, char* scratch,
+                                   size_t scratch_stride, int batch, int n, int ell, int esz,
+                                   uint64_t seed) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= batch) return;
+  HeevdProb p;
+  p.H = (char*)H + (size_t)b * n * n * esz;
+  p.ldh = n;
+  p.n = n;
+  p.ell = ell;
+  p.V = (char*)evecs + (size_t)b * n * ell * esz;
+  p.ldv = ell;
+  p.seed = seed + 0x9E3779B97F4A7C15ull * (uint64_t)b;
+  heevd_assign_scratch_dev(p, scratch + (size_t)b * scratch_stride, esz);
+  probs[b] = p;
+}
+
+template <typename R>
+__global__ void heevd_evals_kernel(const HeevdProb* probs, R* evals, int batch, int ell) {
+  const int b = blockIdx.y;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= batch || t >= ell) return;
+  const HeevdProb p = probs[b];
+  evals[(size_t)b * ell + t] = ((const R*)p.lam)[t] * *((const R*)p.scale);
+}
+}  // namespace
+
+extern "C" size_t agb_heevd_workspace(int dtype, int n, int ell) {
+  const int esz = dtype == AGB_C64 ? 8 : 16;
+  return agb_align(heevd_scratch_bytes(esz, n, ell)) + agb_align(sizeof(HeevdProb)) +
+         agb_align(2 * sizeof(GemmProb));
+}
+
+extern "C" int agb_heevd(int dtype, int batch, int n, int ell, void* H, void* evals, void* evecs,
+                         void* ws, size_t ws_bytes, uint64_t seed, void* stream) {
+  if (dtype != AGB_C64 && dtype != AGB_C128) return AGB_ERR_ARG;
+  if (batch < 0 || n < 0 || ell < 0 || ell > n) return AGB_ERR_ARG;
+  if (n > 1024) return AGB_ERR_UNSUPPORTED;
+  if (batch == 0 || n == 0) return AGB_OK;
+  const int esz = dtype == AGB_C64 ? 8 : 16;
+  const size_t stride = agb_align(heevd_scratch_bytes(esz, n, ell));
+  const size_t need = (size_t)batch * (stride + agb_align(sizeof(HeevdProb)) + agb_align(2 * sizeof(GemmProb)));
+  if (ws_bytes < need) return AGB_ERR_WORKSPACE;
+  char* base = (char*)ws;
+  HeevdProb* probs = (HeevdProb*)base;
+  GemmProb* gp = (GemmProb*)(base + agb_align((size_t)batch * sizeof(HeevdProb)));
+  char* scratch = base + agb_align((size_t)batch * sizeof(HeevdProb)) + agb_align((size_t)batch * 2 * sizeof(GemmProb));
+  cudaStream_t s = (cudaStream_t)stream;
+  heevd_setup_kernel<<<(batch + 127) / 128, 128, 0, s>>>(probs, H, evecs, scratch, stride, batch, n, ell, esz, seed);
+  AGB_CHECK_LAUNCH();
+  int rc = (dtype == AGB_C64) ? launch_heevd<float2>(probs, gp, batch, n, ell, s)
+                              : launch_heevd<double2>(probs, gp, batch, n, ell, s);
+  if (rc) return rc;
+  if (ell > 0) {
+    dim3 g((ell + 127) / 128, batch);
+    if (dtype == AGB_C64) heevd_evals_kernel<float><<<g, 128, 0, s>>>(probs, (float*)evals, batch, ell);
+    else heevd_evals_kernel<double><<<g, 128, 0, s>>>(probs, (double*)evals, batch, ell);
+    AGB_CHECK_LAUNCH();
+  }
+  return AGB_OK;
+}

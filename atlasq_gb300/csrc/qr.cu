@@ -1,0 +1,164 @@
+// Householder QR for the MPS canonicalisation sweeps (sm_103a).
+//
+// Replaces robust_qr / torch.linalg.qr (src/atlas_q/linalg_robust.py:55-76) as
+// used by to_left_canonical (adaptive_mps.py:310-339), canonicalize_right_to_left
+// (mps_pytorch.py:123-152) and to_mixed_canonical (adaptive_mps.py:346-385).
+//
+// One CTA (1024 threads = 128 column lanes x 8 row groups) per matrix.  The
+// matrix op(A) (M x N, op = N or T) is copied into the workspace, reduced with
+// zgeqr2-style reflectors (H_j^H applied from the left), then the thin Q
+// (M x kk, kk = min(M, N)) is formed by applying H_0 ... H_{kk-1} to [I; 0].
+// Outputs: Q [M, kk] and R [kk, N] (upper triangular), or their transposes.
+#include "common.cuh"
+
+namespace {
+
+constexpr int QR_CG = 128, QR_RG = 8;
+
+template <typename CX>
+__global__ void __launch_bounds__(1024) qr_kernel(const CX* __restrict__ Ain, int M, int N, int transA,
+                                                  CX* W, CX* Q, CX* R, int trans_out, CX* tau) {
+  typedef typename cx_traits<CX>::R Rt;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  CX* v = (CX*)smem_raw;                 // [M]
+  CX* part = v + M;                      // [QR_RG][QR_CG]
+  __shared__ Rt red[32];
+  __shared__ CX bc[2];
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int cg = tid % QR_CG, rg = tid / QR_CG;
+  const int kk = M < N ? M : N;
+  // W = op(A), row-major M x N
+  for (int64_t i = tid; i < (int64_t)M * N; i += nt) {
+    const int r = (int)(i / N), c = (int)(i % N);
+    W[i] = transA ? Ain[(int64_t)c * M + r] : Ain[i];
+  }
+  __syncthreads();
+  for (int j = 0; j < kk; ++j) {
+    Rt p = 0;
+    for (int r = j + 1 + tid; r < M; r += nt) p += cabs2(W[(int64_t)r * N + j]);
+    const Rt xn2 = block_sum(p, red);
+    if (tid == 0) {
+      const CX alpha = W[(int64_t)j * N + j];
+      CX t = czero<CX>(), sc = czero<CX>();
+      Rt beta;
+      if (xn2 == Rt(0) && alpha.y == Rt(0)) {
+        beta = alpha.x;
+      } else {
+        beta = -copysign(sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xn2), alpha.x);
+        t = mk<CX>((beta - alpha.x) / beta, -alpha.y / beta);
+        sc = cinv(csub(alpha, mk<CX>(beta, 0)));
+      }
+      bc[0] = t;
+      bc[1] = sc;
+      tau[j] = t;
+      W[(int64_t)j * N + j] = mk<CX>(beta, 0);
+      v[j] = mk<CX>(1, 0);
+    }
+    __syncthreads();
+    const CX t = bc[0], sc = bc[1];
+    for (int r = j + 1 + tid; r < M; r += nt) {
+      const CX x = cmul(W[(int64_t)r * N + j], sc);
+      v[r] = x;
+      W[(int64_t)r * N + j] = x;
+    }
+    __syncthreads();
+    if (t.x == Rt(0) && t.y == Rt(0)) continue;
+    const CX tc = cconj(t);
+    // apply H^H = I - conj(tau) v v^H to columns c > j
+    for (int c0 = j + 1; c0 < N; c0 += QR_CG) {
+      const int c = c0 + cg;
+      CX acc = czero<CX>();
+      if (c < N)
+        for (int r = j + rg; r < M; r += QR_RG) cfmac(acc, v[r], W[(int64_t)r * N + c]);
+      part[rg * QR_CG + cg] = acc;
+      __syncthreads();
+      if (c < N) {
+        CX w = czero<CX>();
+#pragma unroll
+        for (int g = 0; g < QR_RG; ++g) w = cadd(w, part[g * QR_CG + cg]);
+        const CX tw = cmul(tc, w);
+        for (int r = j + rg; r < M; r += QR_RG) {
+          CX* a = W + (int64_t)r * N + c;
+          *a = csub(*a, cmul(v[r], tw));
+        }
+      }
+      __syncthreads();
+    }
+  }
+  // R = upper triangle of W[:kk, :]
+  for (int64_t i = tid; i < (int64_t)kk * N; i += nt) {
+    const int r = (int)(i / N), c = (int)(i % N);
+    const CX val = (c >= r) ? W[(int64_t)r * N + c] : czero<CX>();
+    if (trans_out) R[(int64_t)c * kk + r] = val;
+    else R[i] = val;
+  }
+  // Q = H_0 ... H_{kk-1} [I; 0]: apply the reflectors (stored below the diagonal
+  // of W, unit leading entry) in reverse order to the first kk identity columns.
+  // Element (r, c) of Q lives at r*kk + c, or at c*M + r when transposed.
+  const int64_t qs_r = trans_out ? 1 : kk, qs_c = trans_out ? M : 1;
+  for (int64_t i = tid; i < (int64_t)M * kk; i += nt) {
+    const int r = (int)(i / kk), c = (int)(i % kk);
+    Q[r * qs_r + c * qs_c] = (r == c) ? mk<CX>(1, 0) : czero<CX>();
+  }
+  __syncthreads();
+  for (int j = kk - 1; j >= 0; --j) {
+    const CX t = tau[j];
+    if (t.x == Rt(0) && t.y == Rt(0)) continue;
+    for (int r = j + tid; r < M; r += nt) v[r] = (r == j) ? mk<CX>(1, 0) : W[(int64_t)r * N + j];
+    __syncthreads();
+    for (int c0 = j; c0 < kk; c0 += QR_CG) {
+      const int c = c0 + cg;
+      CX acc = czero<CX>();
+      if (c < kk)
+        for (int r = j + rg; r < M; r += QR_RG) cfmac(acc, v[r], Q[r * qs_r + c * qs_c]);
+      part[rg * QR_CG + cg] = acc;
+      __syncthreads();
+      if (c < kk) {
+        CX w = czero<CX>();
+#pragma unroll
+        for (int g = 0; g < QR_RG; ++g) w = cadd(w, part[g * QR_CG + cg]);
+        const CX tw = cmul(t, w);
+        for (int r = j + rg; r < M; r += QR_RG) {
+          CX* a = Q + r * qs_r + c * qs_c;
+          *a = csub(*a, cmul(v[r], tw));
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" size_t agb_qr_workspace(int dtype, int M, int N) {
+  const int esz = dtype == AGB_C64 ? 8 : 16;
+  const int kk = M < N ? M : N;
+  return agb_align((size_t)M * N * esz) + agb_align((size_t)kk * esz);
+}
+
+extern "C" int agb_qr(int dtype, const void* A, int M, int N, int transA, void* Q, void* R,
+                      int trans_out, void* ws, size_t ws_bytes, void* stream) {
+  if (dtype != AGB_C64 && dtype != AGB_C128) return AGB_ERR_ARG;
+  if (M <= 0 || N <= 0 || !A || !Q || !R || !ws) return AGB_ERR_ARG;
+  if (M > 8192) return AGB_ERR_UNSUPPORTED;
+  if (ws_bytes < agb_qr_workspace(dtype, M, N)) return AGB_ERR_WORKSPACE;
+  const int esz = dtype == AGB_C64 ? 8 : 16;
+  const int kk = M < N ? M : N;
+  char* base = (char*)ws;
+  void* W = base;
+  void* tau = base + agb_align((size_t)M * N * esz);
+  const size_t smem = (size_t)M * esz + (size_t)QR_RG * QR_CG * esz;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (dtype == AGB_C64) {
+    if (smem > 48 * 1024) cudaFuncSetAttribute(qr_kernel<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    qr_kernel<float2><<<1, 1024, smem, s>>>((const float2*)A, M, N, transA, (float2*)W, (float2*)Q,
+                                             (float2*)R, trans_out, (float2*)tau);
+  } else {
+    if (smem > 48 * 1024) cudaFuncSetAttribute(qr_kernel<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    qr_kernel<double2><<<1, 1024, smem, s>>>((const double2*)A, M, N, transA, (double2*)W,
+                                              (double2*)Q, (double2*)R, trans_out, (double2*)tau);
+  }
+  (void)kk;
+  AGB_CHECK_LAUNCH();
+  return AGB_OK;
+}

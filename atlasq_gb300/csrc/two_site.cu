@@ -1,0 +1,469 @@
+// Two-site MPS update for a batch of gates on disjoint bonds (sm_103a).
+//
+// Per gate g (bond i, A = site i [chiL,2,chiM], B = site i+1 [chiM,2,chiR]):
+//   X  = fused contraction + gate          [m = 2chiL, n = 2chiR]
+//   G  = X^H X                             (n x n Hermitian Gram matrix)
+//   V  = top-ell eigenvectors of G         (heevd.cu)
+//   AV = X V ;  sigma_t^2 = ||AV[:, t]||^2 (Rayleigh quotients, sorted)
+//   k  = reference rank rule on sigma (truncation.py:21-83)
+//   A_new = AV[:, :k]  (= U_k S_k: singular values absorbed LEFT, adaptive_mps.py:281-285)
+//   B_new = V[:, :k]^H (= Vh_k)
+// The Gram formulation never divides by a singular value: A_new B_new = X V_k V_k^H
+// is the projection of X onto the kept right singular subspace.
+#include <math.h>
+
+#include "heevd.cuh"
+
+namespace {
+
+struct Slab {
+  size_t X, G, heevd, V, AV, sig2, perm, total;
+};
+
+AGB_HD Slab slab_layout(int m, int n, int ell, int esz) {
+  Slab s;
+  size_t o = 0;
+  s.X = o;     o += agb_align((size_t)m * n * esz);
+  s.G = o;     o += agb_align((size_t)n * n * esz);
+  s.heevd = o; o += agb_align(heevd_scratch_bytes(esz, n, ell));
+  s.V = o;     o += agb_align((size_t)n * ell * esz);
+  s.AV = o;    o += agb_align((size_t)m * ell * esz);
+  s.sig2 = o;  o += agb_align((size_t)ell * sizeof(double));
+  s.perm = o;  o += agb_align((size_t)ell * sizeof(int));
+  s.total = o;
+  return s;
+}
+
+AGB_HD double dbits(int64_t v) {
+  union {
+    int64_t i;
+    double d;
+  } u;
+  u.i = v;
+  return u.d;
+}
+AGB_HD int64_t bitsd(double v) {
+  union {
+    int64_t i;
+    double d;
+  } u;
+  u.d = v;
+  return u.i;
+}
+
+// header of the batch workspace: [HeevdProb x G][GemmProb x 4G][ContractProb x G]
+struct ContractProb {
+  const void* A;
+  const void* B;
+  const void* U;
+  void* X;
+  int chiL, chiM, chiR;
+  int64_t ldx;
+};
+
+AGB_HD size_t header_bytes(int ng) {
+  return agb_align((size_t)ng * sizeof(HeevdProb)) + agb_align((size_t)ng * 4 * sizeof(GemmProb)) +
+         agb_align((size_t)ng * sizeof(ContractProb));
+}
+
+// ------------------------------------------------------------------ setup
+__global__ void setup_kernel(const int64_t* __restrict__ desc, int ng, char* ws, int esz) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= ng) return;
+  const int64_t* D = desc + (int64_t)g * AGB_D_NFIELDS;
+  const int chiL = (int)D[AGB_D_CHIL], chiM = (int)D[AGB_D_CHIM], chiR = (int)D[AGB_D_CHIR];
+  const int m = 2 * chiL, n = 2 * chiR, ell = (int)D[AGB_D_ELL];
+  char* slab = ws + D[AGB_D_WS];
+  const Slab L = slab_layout(m, n, ell, esz);
+  HeevdProb* hp = (HeevdProb*)ws;
+  GemmProb* gp = (GemmProb*)(ws + agb_align((size_t)ng * sizeof(HeevdProb)));
+  ContractProb* cp = (ContractProb*)(ws + agb_align((size_t)ng * sizeof(HeevdProb)) +
+                                     agb_align((size_t)ng * 4 * sizeof(GemmProb)));
+  HeevdProb p;
+  p.H = slab + L.G;
+  p.ldh = n;
+  p.n = n;
+  p.ell = ell;
+  p.V = slab + L.V;
+  p.ldv = ell;
+  p.seed = (uint64_t)D[AGB_D_SEED];
+  heevd_assign_scratch_dev(p, slab + L.heevd, esz);
+  hp[g] = p;
+  // gp[0..2ng) reserved for the eigensolver polish; [2ng, 3ng) Gram; [3ng, 4ng) AV
+  GemmProb gr;
+  gr.A = slab + L.X; gr.B = slab + L.X; gr.D = slab + L.G; gr.Csrc = slab + L.G;
+  gr.lda = n; gr.ldb = n; gr.ldd = n; gr.ldc = n;
+  gr.M = n; gr.N = n; gr.K = m;
+  gr.opA = 2; gr.opB = 0;
+  gr.alpha_re = 1; gr.alpha_im = 0; gr.beta_re = 0; gr.beta_im = 0;
+  gp[2 * ng + g] = gr;
+  GemmProb av;
+  av.A = slab + L.X; av.B = slab + L.V; av.D = slab + L.AV; av.Csrc = slab + L.AV;
+  av.lda = n; av.ldb = ell; av.ldd = ell; av.ldc = ell;
+  av.M = m; av.N = ell; av.K = n;
+  av.opA = 0; av.opB = 0;
+  av.alpha_re = 1; av.alpha_im = 0; av.beta_re = 0; av.beta_im = 0;
+  gp[3 * ng + g] = av;
+  ContractProb c;
+  c.A = (const void*)D[AGB_D_A];
+  c.B = (const void*)D[AGB_D_B];
+  c.U = (const void*)D[AGB_D_U];
+  c.X = slab + L.X;
+  c.chiL = chiL;
+  c.chiM = chiM;
+  c.chiR = chiR;
+  c.ldx = n;
+  cp[g] = c;
+}
+
+// ------------------------------------------------------------------ contraction
+// Tile: 16 left indices l x 16 right indices j, all four (p', q'), K-chunks of 16.
+template <typename CX>
+__global__ void __launch_bounds__(256) contract_gate_kernel(const ContractProb* __restrict__ probs,
+                                                            ContractProb single) {
+  const ContractProb P = probs ? probs[blockIdx.z] : single;
+  const int l0 = blockIdx.y * 16, j0 = blockIdx.x * 16;
+  if (l0 >= P.chiL || j0 >= P.chiR) return;
+  __shared__ CX As[16][2][17];
+  __shared__ CX Bs[16][2][17];
+  __shared__ CX Us[16];
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  const CX* A = (const CX*)P.A;
+  const CX* B = (const CX*)P.B;
+  if (tid < 16) Us[tid] = ((const CX*)P.U)[tid];
+  CX th[2][2];
+  th[0][0] = th[0][1] = th[1][0] = th[1][1] = czero<CX>();
+  const int chiM = P.chiM, chiR = P.chiR, chiL = P.chiL;
+  for (int r0 = 0; r0 < chiM; r0 += 16) {
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+      const int idx = tid + 256 * e;  // 0..511
+      // A[l][p][r]: l = idx / 32, p = (idx / 16) % 2, r = idx % 16
+      {
+        const int l = idx >> 5, pp = (idx >> 4) & 1, r = idx & 15;
+        const int gl = l0 + l, gr = r0 + r;
+        As[l][pp][r] = (gl < chiL && gr < chiM) ? A[((int64_t)gl * 2 + pp) * chiM + gr] : czero<CX>();
+      }
+      // B[r][q][j]: r = idx / 32, q = (idx / 16) % 2, j = idx % 16
+      {
+        const int r = idx >> 5, q = (idx >> 4) & 1, j = idx & 15;
+        const int gr = r0 + r, gj = j0 + j;
+        Bs[r][q][j] = (gr < chiM && gj < chiR) ? B[((int64_t)gr * 2 + q) * chiR + gj] : czero<CX>();
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < 16; ++r) {
+      const CX a0 = As[ty][0][r], a1 = As[ty][1][r];
+      const CX b0 = Bs[r][0][tx], b1 = Bs[r][1][tx];
+      cfma(th[0][0], a0, b0);
+      cfma(th[0][1], a0, b1);
+      cfma(th[1][0], a1, b0);
+      cfma(th[1][1], a1, b1);
+    }
+    __syncthreads();
+  }
+  const int l = l0 + ty, j = j0 + tx;
+  if (l >= chiL || j >= chiR) return;
+  CX* X = (CX*)P.X;
+#pragma unroll
+  for (int p = 0; p < 2; ++p)
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int row = 2 * p + q;
+      CX acc = czero<CX>();
+      cfma(acc, Us[row * 4 + 0], th[0][0]);
+      cfma(acc, Us[row * 4 + 1], th[0][1]);
+      cfma(acc, Us[row * 4 + 2], th[1][0]);
+      cfma(acc, Us[row * 4 + 3], th[1][1]);
+      X[((int64_t)l * 2 + p) * P.ldx + (int64_t)q * chiR + j] = acc;
+    }
+}
+
+// ------------------------------------------------------------------ rank selection
+// One block per gate.  sigma_t^2 = ||AV[:, t]||^2, sorted descending; then the
+// reference rank rule with torch-CPU float32 semantics for complex64:
+//   E = cumsum(S*S) accumulated in double, each partial rounded to float32;
+//   thresh = f32(f32(1 - eps^2) * total); k_tol = searchsorted_left(E, thresh) + 1.
+template <typename CX>
+__global__ void __launch_bounds__(1024) rank_kernel(int64_t* __restrict__ desc, int ng, char* ws) {
+  typedef typename cx_traits<CX>::R R;
+  const bool f32 = sizeof(R) == 4;
+  const int g = blockIdx.x;
+  int64_t* D = desc + (int64_t)g * AGB_D_NFIELDS;
+  const int chiL = (int)D[AGB_D_CHIL], chiR = (int)D[AGB_D_CHIR];
+  const int m = 2 * chiL, n = 2 * chiR, ell = (int)D[AGB_D_ELL], cap = (int)D[AGB_D_CAP];
+  const double eps = dbits(D[AGB_D_EPS]);
+  char* slab = ws + D[AGB_D_WS];
+  const Slab Ls = slab_layout(m, n, ell, sizeof(CX));
+  const CX* X = (const CX*)(slab + Ls.X);
+  const CX* AV = (const CX*)(slab + Ls.AV);
+  double* sig2 = (double*)(slab + Ls.sig2);
+  int* perm = (int*)(slab + Ls.perm);
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double* s_raw = (double*)smem_raw;  // [ell]
+  double* s_sorted = s_raw + ell;     // [ell]
+  __shared__ double red[32];
+  const int tid = threadIdx.x, nt = blockDim.x;
+  // total = ||X||_F^2 in double
+  double part = 0;
+  for (int64_t i = tid; i < (int64_t)m * n; i += nt) part += (double)cabs2(X[i]);
+  const double total_d = block_sum(part, red);
+  for (int t = tid; t < ell; t += nt) {
+    double acc = 0;
+    for (int r = 0; r < m; ++r) acc += (double)cabs2(AV[(int64_t)r * ell + t]);
+    s_raw[t] = f32 ? (double)(float)acc : acc;
+  }
+  __syncthreads();
+  for (int t = tid; t < ell; t += nt) {
+    const double v = s_raw[t];
+    int rk = 0;
+    for (int u = 0; u < ell; ++u) {
+      const double w = s_raw[u];
+      rk += (w > v) || (w == v && u < t);
+    }
+    s_sorted[rk] = v;
+    perm[rk] = t;
+  }
+  __syncthreads();
+  for (int t = tid; t < ell; t += nt) sig2[t] = s_sorted[t];
+  if (tid != 0) return;
+  const int kmax = min(m, n);
+  int k;
+  double eps_local = 0, entropy = 0, condS = INFINITY;
+  int status = AGB_OK, needed = ell;
+  // singular values as the reference sees them: S = sqrt(sigma^2) in working precision
+  if (ell == 0) {
+    k = 0;
+  } else {
+    // total = E[-1] of the reference: when every potentially non-zero pair was
+    // computed (ell == min(m, n)) it is the end of our own cumsum; otherwise the
+    // Frobenius norm of X stands in for the unseen tail.
+    double total;
+    if (ell >= kmax) {
+      double a = 0;
+      for (int t = 0; t < ell; ++t) {
+        if (f32) {
+          const float s = sqrtf((float)s_sorted[t]);
+          a += (double)(s * s);
+        } else {
+          const double s = sqrt(s_sorted[t]);
+          a += s * s;
+        }
+      }
+      total = f32 ? (double)(float)a : a;
+    } else {
+      total = f32 ? (double)(float)total_d : total_d;
+    }
+    if (total < 1e-30) {
+      k = 1;
+      eps_local = 0;
+      entropy = 0;
+      condS = INFINITY;
+    } else {
+      double thresh;
+      if (f32) thresh = (double)(float)((float)(1.0 - eps * eps) * (float)total);
+      else thresh = (1.0 - eps * eps) * total;
+      double acc = 0;
+      int ktol = -1;
+      double Ek = 0;
+      for (int t = 0; t < ell; ++t) {
+        double sq;
+        if (f32) {
+          const float s = sqrtf((float)s_sorted[t]);
+          sq = (double)(s * s);
+        } else {
+          const double s = sqrt(s_sorted[t]);
+          sq = s * s;
+        }
+        acc += sq;
+        const double Et = f32 ? (double)(float)acc : acc;
+        if (Et >= thresh) {
+          ktol = t + 1;
+          break;
+        }
+      }
+      const int full = min(kmax, cap);
+      if (ktol < 0) {
+        if (ell < full) {
+          status = AGB_ERR_RANK;
+          needed = full;
+          ktol = ell;
+        } else {
+          ktol = kmax;
+        }
+      }
+      ktol = min(ktol, kmax);
+      k = min(ktol, cap);
+      k = min(k, ell);
+      // E[k-1]
+      acc = 0;
+      for (int t = 0; t < k; ++t) {
+        if (f32) {
+          const float s = sqrtf((float)s_sorted[t]);
+          acc += (double)(s * s);
+        } else {
+          const double s = sqrt(s_sorted[t]);
+          acc += s * s;
+        }
+      }
+      Ek = f32 ? (double)(float)acc : acc;
+      const double rem = total - Ek;
+      eps_local = f32 ? (double)sqrtf((float)fmax(rem, 0.0)) : sqrt(fmax(rem, 0.0));
+      double ssum = 0;
+      for (int t = 0; t < k; ++t) ssum += s_sorted[t];
+      for (int t = 0; t < k; ++t) {
+        const double p = s_sorted[t] / ssum;
+        entropy -= p * log(fmax(p, 1e-30));
+      }
+      if (k > 1) {
+        if (f32) {
+          const float s0 = sqrtf((float)s_sorted[0]), sk = sqrtf((float)s_sorted[k - 1]);
+          condS = sk > 0.f ? (double)(s0 / sk) : INFINITY;
+        } else {
+          const double s0 = sqrt(s_sorted[0]), sk = sqrt(s_sorted[k - 1]);
+          condS = sk > 0 ? s0 / sk : INFINITY;
+        }
+      }
+    }
+  }
+  D[AGB_D_K] = k;
+  D[AGB_D_EPSLOC] = bitsd(eps_local);
+  D[AGB_D_ENTROPY] = bitsd(entropy);
+  D[AGB_D_CONDS] = bitsd(condS);
+  D[AGB_D_STATUS] = status;
+  D[AGB_D_TOTAL] = bitsd(total_d);
+  D[AGB_D_NEEDED] = needed;
+}
+
+// ------------------------------------------------------------------ scatter
+template <typename CX>
+__global__ void scatter_kernel(const int64_t* __restrict__ desc, char* ws) {
+  const int g = blockIdx.y;
+  const int64_t* D = desc + (int64_t)g * AGB_D_NFIELDS;
+  const int chiL = (int)D[AGB_D_CHIL], chiR = (int)D[AGB_D_CHIR];
+  const int m = 2 * chiL, n = 2 * chiR, ell = (int)D[AGB_D_ELL], k = (int)D[AGB_D_K];
+  char* slab = ws + D[AGB_D_WS];
+  const Slab Ls = slab_layout(m, n, ell, sizeof(CX));
+  const CX* AV = (const CX*)(slab + Ls.AV);
+  const CX* V = (const CX*)(slab + Ls.V);
+  const int* perm = (const int*)(slab + Ls.perm);
+  CX* An = (CX*)D[AGB_D_ANEW];
+  CX* Bn = (CX*)D[AGB_D_BNEW];
+  const int64_t na = (int64_t)m * k, nb = (int64_t)k * n;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < na + nb;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    if (i < na) {
+      const int r = (int)(i / k), j = (int)(i % k);
+      An[i] = AV[(int64_t)r * ell + perm[j]];
+    } else {
+      const int64_t ii = i - na;
+      const int j = (int)(ii / n), c = (int)(ii % n);
+      Bn[ii] = cconj(V[(int64_t)c * ell + perm[j]]);
+    }
+  }
+}
+
+template <typename CX>
+int run_impl(int ng, int64_t* desc, int maxL, int maxM, int maxR, int maxell, char* ws, cudaStream_t s) {
+  const int esz = sizeof(CX);
+  setup_kernel<<<(ng + 127) / 128, 128, 0, s>>>(desc, ng, ws, esz);
+  AGB_CHECK_LAUNCH();
+  HeevdProb* hp = (HeevdProb*)ws;
+  GemmProb* gp = (GemmProb*)(ws + agb_align((size_t)ng * sizeof(HeevdProb)));
+  ContractProb* cp = (ContractProb*)(ws + agb_align((size_t)ng * sizeof(HeevdProb)) +
+                                     agb_align((size_t)ng * 4 * sizeof(GemmProb)));
+  ContractProb none = {};
+  contract_gate_kernel<CX><<<dim3((maxR + 15) / 16, (maxL + 15) / 16, ng), 256, 0, s>>>(cp, none);
+  AGB_CHECK_LAUNCH();
+  const int maxm = 2 * maxL, maxn = 2 * maxR;
+  int rc = launch_gemm_probs<CX>(gp + 2 * ng, ng, maxn, maxn, s);
+  if (rc) return rc;
+  rc = launch_heevd<CX>(hp, gp, ng, maxn, maxell, s);
+  if (rc) return rc;
+  rc = launch_gemm_probs<CX>(gp + 3 * ng, ng, maxm, maxell, s);
+  if (rc) return rc;
+  rank_kernel<CX><<<ng, 1024, 2 * (size_t)maxell * sizeof(double), s>>>(desc, ng, ws);
+  AGB_CHECK_LAUNCH();
+  return AGB_OK;
+}
+
+}  // namespace
+
+extern "C" int agb_version(void) { return 100; }
+
+extern "C" int agb_contract_gate(int dtype, const void* A, const void* B, const void* U, void* X,
+                                 int chiL, int chiM, int chiR, void* stream) {
+  if (dtype != AGB_C64 && dtype != AGB_C128) return AGB_ERR_ARG;
+  if (chiL <= 0 || chiM <= 0 || chiR <= 0 || !A || !B || !U || !X) return AGB_ERR_ARG;
+  ContractProb p;
+  p.A = A;
+  p.B = B;
+  p.U = U;
+  p.X = X;
+  p.chiL = chiL;
+  p.chiM = chiM;
+  p.chiR = chiR;
+  p.ldx = 2 * (int64_t)chiR;
+  cudaStream_t s = (cudaStream_t)stream;
+  dim3 grid((chiR + 15) / 16, (chiL + 15) / 16, 1);
+  if (dtype == AGB_C64) contract_gate_kernel<float2><<<grid, 256, 0, s>>>(nullptr, p);
+  else contract_gate_kernel<double2><<<grid, 256, 0, s>>>(nullptr, p);
+  AGB_CHECK_LAUNCH();
+  return AGB_OK;
+}
+
+extern "C" int agb_two_site_plan(int dtype, int ng, int64_t* desc, size_t* ws_bytes) {
+  if (dtype != AGB_C64 && dtype != AGB_C128) return AGB_ERR_ARG;
+  if (ng < 0 || (ng > 0 && !desc) || !ws_bytes) return AGB_ERR_ARG;
+  const int esz = dtype == AGB_C64 ? 8 : 16;
+  size_t off = header_bytes(ng);
+  for (int g = 0; g < ng; ++g) {
+    int64_t* D = desc + (int64_t)g * AGB_D_NFIELDS;
+    const int chiL = (int)D[AGB_D_CHIL], chiM = (int)D[AGB_D_CHIM], chiR = (int)D[AGB_D_CHIR];
+    const int cap = (int)D[AGB_D_CAP];
+    if (chiL <= 0 || chiM <= 0 || chiR <= 0 || cap <= 0) return AGB_ERR_ARG;
+    const int m = 2 * chiL, n = 2 * chiR;
+    if (n > 1024) return AGB_ERR_UNSUPPORTED;
+    const int full = m < n ? (m < cap ? m : cap) : (n < cap ? n : cap);
+    int ell = (int)D[AGB_D_ELL];
+    if (ell <= 0 || ell > full) ell = full;
+    D[AGB_D_ELL] = ell;
+    D[AGB_D_WS] = (int64_t)off;
+    off += agb_align(slab_layout(m, n, ell, esz).total);
+  }
+  *ws_bytes = off;
+  return AGB_OK;
+}
+
+extern "C" int agb_two_site_run(int dtype, int ng, const int64_t* desc_dev, int64_t* desc_out,
+                                int max_chiL, int max_chiM, int max_chiR, int max_ell, void* ws,
+                                size_t ws_bytes, void* stream) {
+  (void)max_chiM;
+  (void)desc_dev;
+  if (dtype != AGB_C64 && dtype != AGB_C128) return AGB_ERR_ARG;
+  if (ng <= 0) return AGB_OK;
+  if (!desc_out || !ws || max_chiL <= 0 || max_chiR <= 0 || max_ell <= 0) return AGB_ERR_ARG;
+  if (2 * max_chiR > 1024 || max_ell > 1024) return AGB_ERR_UNSUPPORTED;
+  if (ws_bytes < header_bytes(ng)) return AGB_ERR_WORKSPACE;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (dtype == AGB_C64)
+    return run_impl<float2>(ng, desc_out, max_chiL, max_chiM, max_chiR, max_ell, (char*)ws, s);
+  return run_impl<double2>(ng, desc_out, max_chiL, max_chiM, max_chiR, max_ell, (char*)ws, s);
+}
+
+extern "C" int agb_two_site_finalize(int dtype, int ng, const int64_t* desc_dev, int max_chiL,
+                                     int max_chiR, int max_k, void* ws, void* stream) {
+  if (dtype != AGB_C64 && dtype != AGB_C128) return AGB_ERR_ARG;
+  if (ng <= 0) return AGB_OK;
+  if (!desc_dev || !ws) return AGB_ERR_ARG;
+  const int64_t tot = (int64_t)2 * max_chiL * max_k + (int64_t)max_k * 2 * max_chiR;
+  int blocks = (int)((tot + 255) / 256);
+  if (blocks < 1) blocks = 1;
+  if (blocks > 4096) blocks = 4096;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (dtype == AGB_C64) scatter_kernel<float2><<<dim3(blocks, ng), 256, 0, s>>>(desc_dev, (char*)ws);
+  else scatter_kernel<double2><<<dim3(blocks, ng), 256, 0, s>>>(desc_dev, (char*)ws);
+  AGB_CHECK_LAUNCH();
+  return AGB_OK;
+}

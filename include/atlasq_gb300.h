@@ -1,0 +1,147 @@
+/*
+ * atlasq_gb300 -- C ABI of the GB300 (sm_103a) MPS circuit-simulation hot path.
+ *
+ * Drop-in boundary for the matrix-product-state path of ATLAS-Q
+ * (followthesapper/ATLAS-Q 0.7.0).  Every entry point takes plain device
+ * pointers, sizes and a CUDA stream (as void*), never allocates or frees, and
+ * returns an int status (AGB_OK == 0).  Complex numbers are interleaved
+ * (re, im) pairs: complex64 = two floats, complex128 = two doubles -- the same
+ * memory layout as torch.complex64 / torch.complex128 tensors.  Site tensors are
+ * contiguous row-major [chiL, 2, chiR].
+ *
+ * Each entry point names the reference interface it replaces (file:line,
+ * relative to the reference project root).
+ */
+#ifndef ATLASQ_GB300_H
+#define ATLASQ_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status */
+#define AGB_OK 0
+#define AGB_ERR_ARG 1          /* bad shape / argument (reference: assert / ValueError) */
+#define AGB_ERR_WORKSPACE 2    /* workspace smaller than the planned size */
+#define AGB_ERR_NOCONV 3       /* eigensolver residual check failed */
+#define AGB_ERR_TIMEOUT 4      /* a bounded device-side wait expired */
+#define AGB_ERR_CUDA 5         /* CUDA launch / runtime error */
+#define AGB_ERR_UNSUPPORTED 6  /* size or mode not supported by this build */
+#define AGB_ERR_RANK 7         /* eigenpairs computed < rank required (caller re-plans) */
+
+/* dtype codes */
+#define AGB_C64 0
+#define AGB_C128 1
+
+/* ---------------------------------------------------- two-site descriptor
+ * One row of int64 fields per two-site gate of a batch.  Pointers are device
+ * addresses stored as int64; reals are stored as the bits of an IEEE double.
+ * Fields marked (in) are filled by the caller, (plan) by agb_two_site_plan,
+ * (out) by the device.
+ */
+enum agb_desc_field {
+  AGB_D_A = 0,        /* (in)  const site tensor i   [chiL,2,chiM]            */
+  AGB_D_B = 1,        /* (in)  const site tensor i+1 [chiM,2,chiR]            */
+  AGB_D_U = 2,        /* (in)  const gate [4,4] row-major, same dtype          */
+  AGB_D_CHIL = 3,     /* (in)                                                  */
+  AGB_D_CHIM = 4,     /* (in)                                                  */
+  AGB_D_CHIR = 5,     /* (in)                                                  */
+  AGB_D_CAP = 6,      /* (in)  chi_max for this bond                           */
+  AGB_D_EPS = 7,      /* (in)  eps_bond (double bits)                          */
+  AGB_D_ANEW = 8,     /* (in, finalize) output site i   [chiL,2,k]             */
+  AGB_D_BNEW = 9,     /* (in, finalize) output site i+1 [k,2,chiR]             */
+  AGB_D_ELL = 10,     /* (in)  eigenpairs to compute; 0 = min(2chiR, cap)      */
+  AGB_D_SEED = 11,    /* (in)  Philox seed for start vectors                   */
+  AGB_D_WS = 12,      /* (plan) byte offset of this gate's workspace slab      */
+  AGB_D_K = 16,       /* (out) kept rank                                       */
+  AGB_D_EPSLOC = 17,  /* (out) eps_local (double bits)                         */
+  AGB_D_ENTROPY = 18, /* (out) entropy in nats (double bits)                   */
+  AGB_D_CONDS = 19,   /* (out) sigma_0 / sigma_{k-1} (double bits)             */
+  AGB_D_STATUS = 20,  /* (out) per-gate status                                 */
+  AGB_D_TOTAL = 21,   /* (out) ||X||_F^2 (double bits)                         */
+  AGB_D_NEEDED = 22,  /* (out) eigenpairs actually required (fallback sizing)   */
+  AGB_D_NFIELDS = 32
+};
+
+/* Version / build information. */
+int agb_version(void);
+
+/* (a2) Fused contraction + two-qubit gate.
+ * Replaces fused_two_qubit_gate_pytorch (src/triton_kernels/mps_complex.py:343-368)
+ * and its Triton twin (mps_complex.py:221-336).
+ * X[(l,p),(q,j)] = sum_{p'q'} U[2p+q, 2p'+q'] sum_r A[l,p',r] B[r,q',j];
+ * X is row-major [2chiL, 2chiR]. */
+int agb_contract_gate(int dtype, const void* A, const void* B, const void* U, void* X, int chiL,
+                      int chiM, int chiR, void* stream);
+
+/* (a1) Two-site update, batched over gates on disjoint bonds.
+ * Replaces AdaptiveMPS.apply_two_site_gate (src/atlas_q/adaptive_mps.py:182-308)
+ * together with robust_svd (src/atlas_q/linalg_robust.py:17-52) and
+ * choose_rank_from_sigma (src/atlas_q/truncation.py:21-83).
+ *
+ * agb_two_site_plan   fills AGB_D_WS of every row of `desc_host` and returns the
+ *                     workspace bytes needed (the caller allocates it).
+ * agb_two_site_run    contraction -> Gram -> Hermitian eigensolver -> Rayleigh
+ *                     singular values -> rank selection; writes the (out) fields
+ *                     of `desc_dev` (device copy of the planned rows).
+ * agb_two_site_finalize  writes A_new = X V_k (singular values absorbed left, as
+ *                     adaptive_mps.py:281-285) and B_new = V_k^H into the
+ *                     AGB_D_ANEW / AGB_D_BNEW buffers sized from AGB_D_K. */
+int agb_two_site_plan(int dtype, int ngates, int64_t* desc_host, size_t* ws_bytes);
+int agb_two_site_run(int dtype, int ngates, const int64_t* desc_dev, int64_t* desc_dev_out,
+                     int max_chiL, int max_chiM, int max_chiR, int max_ell, void* ws, size_t ws_bytes,
+                     void* stream);
+int agb_two_site_finalize(int dtype, int ngates, const int64_t* desc_dev, int max_chiL, int max_chiR,
+                          int max_k, void* ws, void* stream);
+
+/* (a6) Single-qubit gate, applied as the reference does: T'[a,t,b] = sum_s U[s,t] T[a,s,b]
+ * (U^T; src/atlas_q/adaptive_mps.py:159-180).  In place. */
+int agb_single_qubit_gate(int dtype, void* T, const void* U, int chiL, int chiR, void* stream);
+
+/* Hermitian eigensolver (batched), exposed for robust_svd / tests.
+ * Replaces the torch.linalg.svd call inside robust_svd (linalg_robust.py:37) when
+ * used as X -> Gram -> eigenpairs.  H: [batch, n, n] Hermitian (overwritten);
+ * evals: [batch, ell] descending; evecs: [batch, n, ell] (column t = eigenvector t). */
+size_t agb_heevd_workspace(int dtype, int n, int ell);
+int agb_heevd(int dtype, int batch, int n, int ell, void* H, void* evals, void* evecs, void* ws,
+              size_t ws_bytes, uint64_t seed, void* stream);
+
+/* Householder QR of op(A) (M x N; transA = 1 reads a row-major N x M matrix
+ * transposed).  Q: [M, min(M,N)], R: [min(M,N), N] upper triangular, or their
+ * plain transposes when trans_out = 1.  Replaces robust_qr / torch.linalg.qr
+ * (src/atlas_q/linalg_robust.py:55-76) in the canonical sweeps
+ * (adaptive_mps.py:310-385, mps_pytorch.py:91-152). */
+size_t agb_qr_workspace(int dtype, int M, int N);
+int agb_qr(int dtype, const void* A, int M, int N, int transA, void* Q, void* R, int trans_out,
+           void* ws, size_t ws_bytes, void* stream);
+
+/* (a9) One site of batched sequential-conditional sampling.
+ * Replaces the per-site body of _batch_sweep_sample (src/atlas_q/mps_pytorch.py:282-352)
+ * with torch.multinomial replaced by a Philox4x32-10 stream:
+ * temp [shots, 2chiR] = L @ T.reshape(chiL, 2chiR) (computed by the caller);
+ * outputs bits <<= 1 | outcome, L_new [shots, chiR] (may be NULL on the last site)
+ * and optionally P(0) per shot (pz_out, double; may be NULL). */
+int agb_sample_site(int dtype, const void* temp, int shots, int chiR, int site, uint64_t seed,
+                    uint64_t shot_offset, int64_t* bits, void* Lnew, double* pz_out, void* stream);
+
+/* (a10) MPO mixing step of the expectation sweep (src/atlas_q/mpo_ops.py:1132-1145):
+ * N[R][a][t][B] = sum_{L,s} W[L][s][t][R] M[L][a][s][B]. */
+int agb_mpo_mix(int dtype, const void* M, const void* W, void* N, int Lw, int Rw, int chiA, int chiB,
+                void* stream);
+/* out2[0] + i out2[1] = sum_{r,c} E[r,c] Q[c,r]  (double accumulation; out2 is device memory). */
+int agb_trace_prod(int dtype, const void* E, const void* Q, int n, double* out2, void* stream);
+
+/* Batched complex GEMM (SIMT reference-free kernel, used by the host layer):
+ * C[b] = alpha * op(A[b]) op(B[b]) + beta * C[b]; op: 'N','T','C'. */
+int agb_cgemm_batched(int dtype, char opA, char opB, int batch, int M, int N, int K,
+                      const void* A, int64_t lda, int64_t strideA, const void* B, int64_t ldb,
+                      int64_t strideB, void* C, int64_t ldc, int64_t strideC, double alpha_re,
+                      double alpha_im, double beta_re, double beta_im, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ATLASQ_GB300_H */

@@ -1,0 +1,134 @@
+"""CPU-side checks: the C-ABI library loads and exports every declared symbol,
+host planning logic, error mapping, and host-side policy code.  No kernel is
+launched here."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import ROOT, load_golden, unpack_spectra
+
+import atlasq_gb300
+from atlasq_gb300 import _build, _lib
+
+
+def header_symbols():
+    src = open(os.path.join(ROOT, "include", "atlasq_gb300.h")).read()
+    return sorted(set(re.findall(r"\b(agb_[a-z0-9_]+)\s*\(", src)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    _build.build()
+    return _lib.load(build_if_missing=False)
+
+
+def test_library_exports_every_declared_symbol(lib):
+    declared = header_symbols()
+    assert len(declared) >= 10
+    for name in declared:
+        assert hasattr(lib, name), name
+    assert set(_lib.exported_symbols()) == set(declared)
+
+
+def test_version(lib):
+    assert lib.agb_version() >= 100
+
+
+def _desc(rows):
+    d = torch.zeros(len(rows), _lib.D_NFIELDS, dtype=torch.int64)
+    for g, (l, m, r, cap, ell) in enumerate(rows):
+        d[g, _lib.D_CHIL], d[g, _lib.D_CHIM], d[g, _lib.D_CHIR] = l, m, r
+        d[g, _lib.D_CAP], d[g, _lib.D_ELL] = cap, ell
+    return d
+
+
+def test_two_site_plan_host_logic(lib):
+    d = _desc([(256, 256, 256, 256, 0), (1, 1, 1, 4, 0), (4, 8, 16, 8, 3), (8, 8, 2, 64, 100)])
+    ws = _lib.SZ(0)
+    _lib.check(lib.agb_two_site_plan(_lib.AGB_C64, 4, _lib.ptr(d), ws))
+    ells = d[:, _lib.D_ELL].tolist()
+    assert ells == [256, 2, 3, 4]          # min(2chiL, 2chiR, cap) or the requested ell
+    offs = d[:, _lib.D_WS].tolist()
+    assert offs == sorted(offs) and all(o % 256 == 0 for o in offs)
+    assert ws.value > offs[-1]
+    # 512x512 Gram slab needs at least X + G complex64 planes
+    assert offs[1] - offs[0] >= 2 * 512 * 512 * 8
+    ws128 = _lib.SZ(0)
+    d2 = _desc([(256, 256, 256, 256, 0)])
+    _lib.check(lib.agb_two_site_plan(_lib.AGB_C128, 1, _lib.ptr(d2), ws128))
+    assert ws128.value > ws.value - offs[1] + offs[0]
+
+
+def test_plan_rejects_bad_shapes(lib):
+    ws = _lib.SZ(0)
+    d = _desc([(0, 2, 2, 4, 0)])
+    assert lib.agb_two_site_plan(_lib.AGB_C64, 1, _lib.ptr(d), ws) == _lib.AGB_ERR_ARG
+    d = _desc([(2, 2, 600, 1024, 0)])
+    assert lib.agb_two_site_plan(_lib.AGB_C64, 1, _lib.ptr(d), ws) == _lib.AGB_ERR_UNSUPPORTED
+    assert lib.agb_two_site_plan(7, 1, _lib.ptr(d), ws) == _lib.AGB_ERR_ARG
+    with pytest.raises(ValueError):
+        _lib.check(_lib.AGB_ERR_ARG, "x")
+    with pytest.raises(NotImplementedError):
+        _lib.check(_lib.AGB_ERR_UNSUPPORTED, "x")
+
+
+def test_entry_points_validate_arguments_without_a_gpu(lib):
+    # argument checks return before any CUDA call
+    assert lib.agb_contract_gate(5, None, None, None, None, 1, 1, 1, None) == _lib.AGB_ERR_ARG
+    assert lib.agb_single_qubit_gate(0, None, None, 1, 1, None) == _lib.AGB_ERR_ARG
+    assert lib.agb_heevd(0, 1, 4, 5, None, None, None, None, 0, 0, None) == _lib.AGB_ERR_ARG
+    assert lib.agb_qr(0, None, 4, 4, 0, None, None, 0, None, 0, None) == _lib.AGB_ERR_ARG
+    assert lib.agb_cgemm_batched(0, b"X", b"N", 1, 1, 1, 1, None, 1, 1, None, 1, 1, None, 1, 1,
+                                 1.0, 0.0, 0.0, 0.0, None) == _lib.AGB_ERR_ARG
+    assert lib.agb_heevd_workspace(0, 512, 272) > 512 * 272 * 8
+
+
+@pytest.mark.skipif(torch.cuda.is_available(), reason="checks the no-GPU failure mode")
+def test_product_path_fails_loudly_without_cuda():
+    with pytest.raises(RuntimeError):
+        atlasq_gb300.AdaptiveMPS(4, bond_dim=1, device="cuda")
+    with pytest.raises(RuntimeError):
+        atlasq_gb300.AdaptiveMPS(4, bond_dim=1, device="cpu")
+
+
+def test_host_choose_rank_matches_reference():
+    g = load_golden("choose_rank")
+    vecs = unpack_spectra(g["lens"], g["flat"])
+    for S, (eps, cap, k, el, ent, cond) in zip(vecs, g["meta"]):
+        k2, el2, ent2, cond2 = atlasq_gb300.choose_rank_from_sigma(torch.tensor(S), eps, int(cap))
+        assert k2 == int(k)
+        assert abs(el2 - el) <= 1e-6 * max(1.0, abs(el)) + 1e-12
+        assert abs(ent2 - ent) <= 1e-5 * max(1.0, abs(ent))
+
+
+def test_statistics_api_matches_reference_semantics():
+    st = atlasq_gb300.MPSStatistics()
+    st.record(step=0, bond=0, k_star=4, chi_before=8, chi_after=4, eps_local=1e-6, entropy=1.5,
+              svd_driver="gb300_gram_heevd", dtype="complex64", ms_elapsed=10.0, condS=100.0)
+    st.record(step=1, bond=1, k_star=6, chi_before=8, chi_after=6, eps_local=2e-6, entropy=2.0,
+              svd_driver="gb300_gram_heevd", dtype="complex64", ms_elapsed=12.0, condS=150.0)
+    s = st.summary()
+    assert s["total_operations"] == 2 and s["max_chi"] == 6 and s["total_time_ms"] == 22.0
+    assert s["cuda_svd_pct"] == 100.0 and s["cpu_fallback_pct"] == 0.0
+    assert abs(st.global_error_bound() - np.sqrt(1e-12 + 4e-12)) < 1e-15
+    assert abs(atlasq_gb300.bond_entropy_from_S(torch.ones(4) / 2.0) - 2.0) < 1e-6
+    assert atlasq_gb300.effective_rank(torch.tensor([1.0, 0.1, 0.01, 0.001]), 0.99) <= 2
+    assert set(atlasq_gb300.get_adaptive_mps()) >= {"AdaptiveMPS", "robust_svd", "choose_rank_from_sigma"}
+
+
+def test_circuit_generators_are_deterministic():
+    from atlasq_gb300.circuits import count_two_site, haar_brickwork, hea_circuit, layers_of
+    a = haar_brickwork(40, 20, seed=1234)
+    b = haar_brickwork(40, 20, seed=1234)
+    assert count_two_site(a) == 390
+    assert all(torch.equal(x[2], y[2]) for x, y in zip(a, b))
+    U = a[0][2].to(torch.complex128)
+    assert torch.allclose(U.conj().T @ U, torch.eye(4, dtype=torch.complex128), atol=1e-6)
+    h = hea_circuit(64, 12, seed=3)
+    assert count_two_site(h) == 756
+    lays = layers_of(a)
+    assert len(lays) == 20 and sum(len(x) for x in lays) == 390

@@ -1,0 +1,379 @@
+"""GPU parity tests: every kernel through the C ABI against the CPU oracle and the
+reference's golden vectors.  Tolerances are written in each test:
+  * contraction / GEMM / single-qubit gate: relative 1e-5 (complex64), 1e-12 (complex128)
+  * eigensolver: residual ||HV - V diag(w)|| <= 5e-5 ||H||, ||V^H V - I|| <= 1e-5
+  * two-site update vs reference: kept singular values within 1e-5 * sigma_0,
+    identical bond dimensions, state fidelity >= 1 - 1e-6.
+"""
+import numpy as np
+import pytest
+import torch
+
+from conftest import load_golden, unpack_spectra, unpack_tensors
+
+pytestmark = pytest.mark.gpu
+
+if not torch.cuda.is_available():
+    pytest.skip("needs a CUDA GPU", allow_module_level=True)
+
+import atlasq_gb300 as aq  # noqa: E402
+from atlasq_gb300 import ops  # noqa: E402
+from atlasq_gb300.circuits import haar_brickwork, haar_unitary, hea_circuit  # noqa: E402
+from oracle import mps_oracle as mo  # noqa: E402
+from oracle import statevector as sv  # noqa: E402
+
+DEV = "cuda:0"
+
+
+def crandn(*shape, dtype=torch.complex64, gen=None):
+    re = torch.randn(*shape, generator=gen, dtype=torch.float64)
+    im = torch.randn(*shape, generator=gen, dtype=torch.float64)
+    return torch.complex(re, im).to(dtype)
+
+
+def rel(a, b):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+# ----------------------------------------------------------------------------- kernels
+@pytest.mark.parametrize("chiL,chiM,chiR", [(1, 1, 1), (1, 2, 4), (3, 5, 7), (17, 33, 9), (64, 64, 64),
+                                            (255, 17, 130)])
+@pytest.mark.parametrize("dt", [torch.complex64, torch.complex128])
+def test_contract_gate_matches_oracle(chiL, chiM, chiR, dt):
+    g = torch.Generator().manual_seed(chiL * 1000 + chiM * 10 + chiR)
+    A = crandn(chiL, 2, chiM, gen=g, dtype=dt)
+    B = crandn(chiM, 2, chiR, gen=g, dtype=dt)
+    U = haar_unitary(g).to(dt)
+    X = ops.contract_gate(A.to(DEV), B.to(DEV), U.to(DEV)).cpu().numpy()
+    ref = mo.fused_two_qubit_gate(A.numpy().astype(np.complex128), B.numpy().astype(np.complex128),
+                                  U.numpy().astype(np.complex128))
+    tol = 1e-5 if dt == torch.complex64 else 1e-12
+    assert rel(X, ref) < tol
+
+
+@pytest.mark.parametrize("opA,opB", [("N", "N"), ("C", "N"), ("N", "C"), ("T", "N"), ("N", "T"), ("C", "C")])
+def test_cgemm_ops(opA, opB):
+    g = torch.Generator().manual_seed(3)
+    M, N, K = 70, 45, 129
+    A = crandn(*((M, K) if opA == "N" else (K, M)), gen=g)
+    B = crandn(*((K, N) if opB == "N" else (N, K)), gen=g)
+    C = ops.cgemm(A.to(DEV), B.to(DEV), opA, opB).cpu().numpy()
+    f = {"N": lambda x: x, "T": lambda x: x.T, "C": lambda x: x.conj().T}
+    ref = f[opA](A.numpy().astype(np.complex128)) @ f[opB](B.numpy().astype(np.complex128))
+    assert rel(C, ref) < 1e-5
+
+
+def _hermitian_cases():
+    g = torch.Generator().manual_seed(11)
+    cases = []
+    for n in (1, 2, 5, 33, 128, 300):
+        X = crandn(n + 3, n, gen=g, dtype=torch.complex128)
+        cases.append(("gram", X.conj().T @ X))
+    # rank deficient Gram (rank 40 of 96)
+    X = crandn(40, 96, gen=g, dtype=torch.complex128)
+    cases.append(("rankdef", X.conj().T @ X))
+    # exactly degenerate spectrum (cluster of 30 equal eigenvalues)
+    Q, _ = torch.linalg.qr(crandn(80, 80, gen=g, dtype=torch.complex128))
+    w = torch.cat([torch.full((30,), 2.0), torch.linspace(1.0, 0.01, 50)]).to(torch.complex128)
+    cases.append(("degenerate", (Q * w) @ Q.conj().T))
+    # graded spectrum over 8 decades
+    w = (10.0 ** -torch.linspace(0, 8, 64)).to(torch.complex128)
+    Q, _ = torch.linalg.qr(crandn(64, 64, gen=g, dtype=torch.complex128))
+    cases.append(("graded", (Q * w) @ Q.conj().T))
+    return cases
+
+
+@pytest.mark.parametrize("case", range(9))
+@pytest.mark.parametrize("dt", [torch.complex64, torch.complex128])
+def test_heevd_residual_and_orthonormality(case, dt):
+    name, H = _hermitian_cases()[case]
+    H = (H + H.conj().T) / 2
+    n = H.shape[0]
+    ell = n if name != "gram" or n < 100 else n // 2
+    w, V = ops.heevd(H.to(dt).to(DEV), ell=ell)
+    w = w.cpu().double().numpy()
+    V = V.cpu().to(torch.complex128).numpy()
+    Hn = H.numpy()
+    ref = np.linalg.eigvalsh(Hn)[::-1][:ell]
+    nrm = np.abs(ref).max()
+    tol = 5e-5 if dt == torch.complex64 else 1e-11
+    assert np.max(np.abs(w - ref)) <= tol * nrm
+    assert np.linalg.norm(Hn @ V - V * w[None, :]) <= tol * nrm * np.sqrt(ell)
+    assert np.max(np.abs(V.conj().T @ V - np.eye(ell))) <= (1e-5 if dt == torch.complex64 else 1e-12)
+
+
+@pytest.mark.parametrize("M,N,trans", [(8, 4, False), (4, 8, False), (512, 256, False), (37, 37, False),
+                                       (256, 512, True), (16, 64, True)])
+def test_qr(M, N, trans):
+    g = torch.Generator().manual_seed(M + N)
+    A = crandn(*((N, M) if trans else (M, N)), gen=g)
+    if M > 20 and not trans:
+        A[:, 3] = A[:, 1] * 2.0  # rank deficiency
+    Q, R = ops.qr(A.to(DEV), transA=trans, trans_out=trans)
+    Q = Q.cpu().to(torch.complex128).numpy()
+    R = R.cpu().to(torch.complex128).numpy()
+    if trans:
+        Q, R = Q.T, R.T
+    Aop = A.numpy().astype(np.complex128)
+    Aop = Aop.T if trans else Aop
+    kk = min(M, N)
+    assert Q.shape == (M, kk) and R.shape == (kk, N)
+    assert rel(Q @ R, Aop) < 1e-5
+    assert np.max(np.abs(Q.conj().T @ Q - np.eye(kk))) < 1e-5
+    assert np.allclose(np.tril(R, -1), 0)
+
+
+def test_single_qubit_gate_uses_transpose_convention():
+    g = load_golden("known_answers")
+    m = aq.AdaptiveMPS(2, bond_dim=1, device=DEV)
+    th = 0.7
+    m.ry(0, th)
+    assert np.allclose(m.to_statevector().cpu().numpy(), g["ry07_state"], atol=1e-6)
+
+
+# ----------------------------------------------------------------------------- two-site update
+CIRCUITS = {
+    "brickwork_n12_d10_chi32": lambda: haar_brickwork(12, 10, seed=1234),
+    "brickwork_n8_d6_chi8": lambda: haar_brickwork(8, 6, seed=5),
+    "brickwork_n10_d8_chi16_eps1e-3": lambda: haar_brickwork(10, 8, seed=11),
+    "hea_n10_l3_chi16": lambda: hea_circuit(10, 3, seed=3),
+}
+
+
+def run_gpu(ops_, n, chi, eps, dtype=torch.complex64, flush_each=False):
+    pol = aq.DTypePolicy(default=dtype)
+    m = aq.AdaptiveMPS(n, bond_dim=1, eps_bond=eps, chi_max_per_bond=chi, device=DEV, dtype=dtype,
+                       dtype_policy=pol)
+    for kind, q, U in ops_:
+        if kind == "2q":
+            m.apply_two_site_gate(q, U)
+        else:
+            m.apply_single_qubit_gate(q, U)
+        if flush_each:
+            m.flush()
+    m.flush()
+    return m
+
+
+@pytest.mark.parametrize("name", sorted(CIRCUITS))
+def test_two_site_matches_reference_golden(name):
+    g = load_golden(name)
+    n, chi, eps = int(g["n"]), int(g["chi"]), float(g["eps"])
+    m = run_gpu(CIRCUITS[name](), n, chi, eps)
+    assert list(m.bond_dims) == list(g["bond_dims"])
+    logs = m.statistics.logs
+    assert logs["k_star"] == [int(x) for x in g["log_k_star"]]
+    ref_eps = g["log_eps_local"]
+    assert np.allclose(logs["eps_local"], ref_eps, atol=2e-6)
+    assert np.allclose(logs["entropy"], g["log_entropy"], atol=1e-4)
+    f = sv.fidelity(m.to_statevector().cpu().numpy(), g["statevector"])
+    assert f > 1 - 1e-6, f
+
+
+@pytest.mark.parametrize("name", sorted(CIRCUITS))
+def test_two_site_fp64_matches_reference_fp64(name):
+    g = load_golden(name)
+    n, chi, eps = int(g["n"]), int(g["chi"]), float(g["eps"])
+    m = run_gpu(CIRCUITS[name](), n, chi, eps, dtype=torch.complex128)
+    assert list(m.bond_dims) == list(g["bond_dims64"])
+    f = sv.fidelity(m.to_statevector().cpu().numpy(), g["statevector64"])
+    assert f > 1 - 1e-10, f
+
+
+def test_batched_equals_one_by_one():
+    ops_ = haar_brickwork(10, 6, seed=21)
+    a = run_gpu(ops_, 10, 16, 1e-8)
+    b = run_gpu(ops_, 10, 16, 1e-8, flush_each=True)
+    assert a.bond_dims == b.bond_dims
+    f = mo.mps_fidelity([t.cpu().numpy() for t in a.tensors], [t.cpu().numpy() for t in b.tensors])
+    assert f > 1 - 1e-10
+
+
+def test_bell_ghz_known_answers():
+    g = load_golden("known_answers")
+    m = aq.AdaptiveMPS(2, bond_dim=1, eps_bond=1e-10, chi_max_per_bond=4, device=DEV)
+    m.h(0)
+    m.cnot(0, 1)
+    assert np.allclose(m.to_statevector().cpu().numpy(), g["bell_state"], atol=1e-6)
+    assert m.bond_dims == [2]
+    assert m.global_error_bound() < 1e-5
+    m = aq.AdaptiveMPS(6, bond_dim=1, eps_bond=1e-10, chi_max_per_bond=8, device=DEV)
+    m.h(0)
+    for i in range(5):
+        m.cnot(i, i + 1)
+    assert sv.fidelity(m.to_statevector().cpu().numpy(), g["ghz6_state"]) > 1 - 1e-6
+    assert m.bond_dims == list(g["ghz6_bonds"])
+    m = aq.AdaptiveMPS(2, bond_dim=1, eps_bond=1e-10, chi_max_per_bond=4, device=DEV)
+    m.apply_two_site_gate(0, torch.tensor(g["u4"]))
+    assert np.allclose(m.to_statevector().cpu().numpy(), g["u4"][:, 0], atol=1e-5)
+
+
+def test_initial_state_shapes_match_reference():
+    m = aq.AdaptiveMPS(5, bond_dim=8, device=DEV)
+    assert m.bond_dims == [2, 4, 8, 8]
+    psi = m.to_statevector().cpu().numpy()
+    assert abs(psi[0] - 1) < 1e-6 and np.abs(psi[1:]).max() < 1e-6
+    m = aq.AdaptiveMPS(4, bond_dim=2, device=DEV)
+    assert m.bond_dims == [2, 2, 2]
+
+
+def test_caps_and_budget_respected():
+    ops_ = haar_brickwork(10, 8, seed=4)
+    m = run_gpu(ops_, 10, 6, 1e-10)
+    assert max(m.bond_dims) <= 6
+    caps = [2, 3, 4, 5, 6, 5, 4, 3, 2]
+    mm = aq.AdaptiveMPS(10, bond_dim=1, eps_bond=1e-10, chi_max_per_bond=caps, device=DEV)
+    for kind, q, U in ops_:
+        mm.apply_two_site_gate(q, U)
+    assert all(d <= c for d, c in zip(mm.bond_dims, caps))
+
+
+def test_fp64_oracle_fidelity_medium():
+    """16 qubits, brickwork depth 12, chi 64: GPU complex64 vs FP64 oracle and exact state."""
+    n, depth, chi = 16, 12, 64
+    ops_ = haar_brickwork(n, depth, seed=99)
+    m = run_gpu(ops_, n, chi, 1e-8)
+    ref = mo.OracleMPS(n, bond_dim=1, eps_bond=1e-8, chi_max_per_bond=chi, dtype=np.complex128)
+    for kind, q, U in ops_:
+        ref.apply_two_site_gate(q, U.numpy())
+    f = mo.mps_fidelity([t.cpu().numpy() for t in m.tensors], ref.tensors)
+    assert f > 1 - 1e-6, f
+    psi = sv.zero_state(n)
+    for kind, q, U in ops_:
+        psi = sv.apply_two_qubit(psi, n, q, U.numpy().astype(np.complex128))
+    fe = sv.fidelity(m.to_statevector().cpu().numpy(), psi)
+    fo = sv.fidelity(ref.to_statevector(), psi)
+    assert abs(fe - fo) < 1e-6
+
+
+# ----------------------------------------------------------------------------- canonical forms
+def test_canonical_sweeps():
+    g = load_golden("canonical")
+    ts = unpack_tensors(g["in_shapes"], g["in_flat"])
+    n = len(ts)
+    m = aq.AdaptiveMPS(n, bond_dim=1, device=DEV)
+    m.tensors = [torch.tensor(t).to(DEV) for t in ts]
+    m.bond_dims = [t.shape[2] for t in ts[:-1]]
+    m.canonicalize_right_to_left()
+    assert sv.fidelity(m.to_statevector().cpu().numpy(), g["right"]) > 1 - 1e-6
+    for t in m.tensors[1:]:
+        M = t.cpu().to(torch.complex128).reshape(t.shape[0], -1).numpy()
+        assert np.allclose(M @ M.conj().T, np.eye(M.shape[0]), atol=1e-5)
+    m.to_mixed_canonical(3)
+    assert sv.fidelity(m.to_statevector().cpu().numpy(), g["mixed"]) > 1 - 1e-6
+    m.to_left_canonical()
+    for t in m.tensors[:-1]:
+        M = t.cpu().to(torch.complex128).reshape(-1, t.shape[2]).numpy()
+        assert np.allclose(M.conj().T @ M, np.eye(M.shape[1]), atol=1e-5)
+    assert sv.fidelity(m.to_statevector().cpu().numpy(), g["left"]) > 1 - 1e-6
+
+
+# ----------------------------------------------------------------------------- sampling
+def test_sampling_bit_exact_vs_oracle():
+    """Same right-canonical tensors, same Philox stream: decisions agree except
+    where |u - P(0)| is below the float32 probability resolution."""
+    from atlasq_gb300.sampling import sample_tensors
+    from oracle.philox import sample_uniforms
+    g = load_golden("canonical")
+    ts = unpack_tensors(g["in_shapes"], g["in_flat"])
+    rc = mo.right_canonicalize(ts)
+    shots, seed = 20000, 77
+    bits, pz = sample_tensors([torch.tensor(t.astype(np.complex64)).to(DEV) for t in rc], shots, seed,
+                              return_pz=True)
+    bits = bits.cpu().numpy()
+    ref_bits, ref_pz = mo.batch_sweep_sample(rc, shots, seed)
+    n = len(rc)
+    diff = bits != ref_bits
+    if diff.any():
+        # every disagreeing shot must have a near-threshold decision somewhere
+        for s in np.nonzero(diff)[0]:
+            near = min(abs(sample_uniforms(seed, np.array([s]), i)[0] - ref_pz[s, i]) for i in range(n))
+            assert near < 1e-5
+    assert diff.mean() < 1e-3
+    p = np.abs(g["before"].astype(np.complex128)) ** 2
+    p /= p.sum()
+    h = np.bincount(bits, minlength=2 ** n) / shots
+    assert 0.5 * np.abs(h - p).sum() < 0.05
+
+
+def test_sample_api_distribution():
+    ops_ = haar_brickwork(8, 6, seed=5)
+    m = run_gpu(ops_, 8, 16, 1e-10)
+    psi = m.to_statevector().cpu().numpy()
+    p = np.abs(psi) ** 2
+    p /= p.sum()
+    s = m.sample(30000, seed=5)
+    h = np.bincount(np.array(s), minlength=256) / len(s)
+    assert 0.5 * np.abs(h - p).sum() < 0.05
+
+
+# ----------------------------------------------------------------------------- expectations
+def test_expectations_match_reference_golden():
+    g = load_golden("expectations")
+    n = int(g["n"])
+    ts = unpack_tensors(g["tensor_shapes"], g["tensor_flat"])
+    m = aq.AdaptiveMPS(n, bond_dim=1, device=DEV)
+    m.tensors = [torch.tensor(t).to(DEV) for t in ts]
+    m.bond_dims = [t.shape[2] for t in ts[:-1]]
+    X = torch.tensor([[0, 1], [1, 0]], dtype=torch.complex64)
+    Y = torch.tensor([[0, -1j], [1j, 0]], dtype=torch.complex64)
+    Z = torch.tensor([[1, 0], [0, -1]], dtype=torch.complex64)
+    for i in range(n - 1):
+        assert abs(aq.correlation_function(Z, i, Z, i + 1, m) - g["zz"][i]) < 1e-5
+    for i in range(n):
+        assert abs(aq.expectation_value(aq.MPOBuilder.local_operator(X, i, n, device=DEV), m) - g["x"][i]) < 1e-5
+        assert abs(aq.expectation_value(aq.MPOBuilder.local_operator(Y, i, n, device=DEV), m) - g["y"][i]) < 1e-5
+    obs = [{i: Z, i + 1: Z} for i in range(n - 1)] + [{i: X} for i in range(n)] + \
+          [{i: X, i + 2: Y} for i in range(n - 2)]
+    vals = aq.local_expectations(m, obs)
+    ref = list(g["zz"]) + list(g["x"]) + list(g["xy"])
+    assert max(abs(a - b) for a, b in zip(vals, ref)) < 1e-5
+
+
+def test_mpo_known_answers():
+    Z = torch.tensor([[1, 0], [0, -1]], dtype=torch.complex64)
+    X = torch.tensor([[0, 1], [1, 0]], dtype=torch.complex64)
+    m = aq.AdaptiveMPS(5, bond_dim=2, device=DEV)
+    assert abs(aq.expectation_value(aq.MPOBuilder.identity_mpo(5, device=DEV), m) - 1.0) < 1e-5
+    assert abs(aq.correlation_function(Z, 0, Z, 2, m).real - 1.0) < 1e-5
+    m = aq.AdaptiveMPS(3, bond_dim=2, device=DEV)
+    m.x(1)
+    assert abs(aq.expectation_value(aq.MPOBuilder.local_operator(Z, 1, 3, device=DEV), m) + 1.0) < 1e-5
+    m = aq.AdaptiveMPS(10, bond_dim=2, device=DEV)
+    for q in range(10):
+        m.h(q)
+    assert abs(aq.correlation_function(X, 0, X, 5, m).real - 1.0) < 1e-4
+    # sum of local operators (MPO bond dimension > 1)
+    Mz = aq.MPOBuilder.sum_local_operators(5, [(i, Z) for i in range(5)], device=DEV)
+    m = aq.AdaptiveMPS(5, bond_dim=1, device=DEV)
+    m.x(2)
+    assert abs(aq.expectation_value(Mz, m) - 3.0) < 1e-4
+
+
+# ----------------------------------------------------------------------------- misc API
+def test_snapshot_roundtrip(tmp_path):
+    ops_ = haar_brickwork(8, 4, seed=8)
+    m = run_gpu(ops_, 8, 16, 1e-8)
+    p = tmp_path / "s.pt"
+    m.snapshot(str(p))
+    m2 = aq.AdaptiveMPS.load_snapshot(str(p), device=DEV)
+    assert m2.bond_dims == m.bond_dims
+    assert sv.fidelity(m.to_statevector().cpu().numpy(), m2.to_statevector().cpu().numpy()) > 1 - 1e-10
+    assert m2.statistics.logs["k_star"] == m.statistics.logs["k_star"]
+
+
+def test_amplitudes_and_robust_svd():
+    ops_ = haar_brickwork(6, 4, seed=2)
+    m = run_gpu(ops_, 6, 16, 1e-10)
+    psi = m.to_statevector().cpu().numpy()
+    for b in (0, 5, 17, 63):
+        assert abs(m.get_amplitude(b) - psi[b]) < 1e-5
+    g = torch.Generator().manual_seed(5)
+    X = crandn(40, 24, gen=g).to(DEV)
+    U, S, Vh, drv = aq.robust_svd(X)
+    ref = np.linalg.svd(X.cpu().numpy().astype(np.complex128), compute_uv=False)
+    assert np.max(np.abs(S.cpu().numpy() - ref)) < 1e-5 * ref[0]
+    assert rel(((U * S.to(U.dtype)) @ Vh).cpu().numpy(), X.cpu().numpy()) < 1e-5
+    assert drv == "gb300_gram_heevd"
