@@ -29,6 +29,9 @@ D_ANEW, D_BNEW, D_ELL, D_SEED, D_WS = 8, 9, 10, 11, 12
 D_K, D_EPSLOC, D_ENTROPY, D_CONDS, D_STATUS, D_TOTAL, D_NEEDED = 16, 17, 18, 19, 20, 21, 22
 D_NFIELDS = 32
 
+STAGES = ["host_gap", "setup", "contract", "gram", "tridiag", "bisect", "invit", "cluster",
+          "backtransform", "polish", "xv", "rank", "scatter"]
+
 _ERRS = {
     AGB_ERR_ARG: (ValueError, "invalid argument or shape"),
     AGB_ERR_WORKSPACE: (RuntimeError, "workspace too small"),
@@ -62,6 +65,9 @@ _SIGS = {
     "agb_sample_site": (I, [I, P, I, I, I, U64, U64, P, P, P, P]),
     "agb_mpo_mix": (I, [I, P, P, P, I, I, I, I, P]),
     "agb_trace_prod": (I, [I, P, P, I, P, P]),
+    "agb_prof_begin": (I, [I]),
+    "agb_launch_count": (ctypes.c_longlong, []),
+    "agb_prof_end": (I, [P, P, I]),
     "agb_cgemm_batched": (I, [I, ctypes.c_char, ctypes.c_char, I, I, I, I, P, I64, I64, P, I64, I64,
                               P, I64, I64, D, D, D, D, P]),
 }

@@ -244,8 +244,11 @@ class AdaptiveMPS:
         G = len(gates)
         desc = torch.zeros(G, _lib.D_NFIELDS, dtype=torch.int64)
         keep = []
-        Us = torch.stack([U.to(dtype=dt, device="cpu") if U.device.type == "cpu" else U.to(dtype=dt).cpu()
-                          for _, U in gates]).contiguous().to(self.device)
+        if all(U.device == self.device for _, U in gates):
+            Us = torch.stack([U.to(dtype=dt) for _, U in gates]).contiguous()
+        else:
+            Us = torch.stack([U.to(dtype=dt, device="cpu") for _, U in gates]).contiguous()
+            Us = Us.to(self.device, non_blocking=True)
         keep.append(Us)
         maxL = maxM = maxR = 1
         meta = []

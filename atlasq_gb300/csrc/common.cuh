@@ -119,8 +119,12 @@ AGB_DEV float philox_normal(uint64_t seed, uint64_t idx, uint32_t stream) {
 
 AGB_HD size_t agb_align(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// Counts kernel launches issued by this library (read with agb_launch_count).
+void agb_note_launch();
+
 #define AGB_CHECK_LAUNCH()                      \
   do {                                          \
+    agb_note_launch();                          \
     cudaError_t _e = cudaGetLastError();        \
     if (_e != cudaSuccess) return AGB_ERR_CUDA; \
   } while (0)

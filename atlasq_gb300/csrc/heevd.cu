@@ -2,6 +2,7 @@
 #include <float.h>
 
 #include "heevd.cuh"
+#include "prof.cuh"
 
 template <typename R> struct rlim;
 template <> struct rlim<float> {
@@ -267,7 +268,7 @@ __global__ void __launch_bounds__(128) invit_kernel(const HeevdProb* __restrict_
   }
   __syncthreads();
   const int t = blockIdx.x * 128 + threadIdx.x;
-  if (t >= ell) return;
+  if (t >= ell || P.skip_vectors) return;
   const R lam = ((const R*)P.lam)[t];
   R tnorm = 0;
   for (int i = 0; i < n; ++i) tnorm = fmax(tnorm, fabs(d[i]) + fabs(e[i]) + (i ? fabs(e[i - 1]) : R(0)));
@@ -359,7 +360,7 @@ template <typename R>
 __global__ void __launch_bounds__(256) cluster_mgs_kernel(const HeevdProb* __restrict__ probs, double tolrel) {
   const HeevdProb P = probs[blockIdx.x];
   const int n = P.n, ell = P.ell;
-  if (ell < 2) return;
+  if (ell < 2 || P.skip_vectors) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   int* start = (int*)smem_raw;  // cluster start for each index
   const R* lam = (const R*)P.lam;
@@ -405,56 +406,7 @@ __global__ void __launch_bounds__(256) cluster_mgs_kernel(const HeevdProb* __res
   }
 }
 
-// ------------------------------------------------------------------ stage 5
-template <typename CX, int NK>
-__global__ void __launch_bounds__(256) backtransform_kernel(const HeevdProb* __restrict__ probs) {
-  typedef typename cx_traits<CX>::R R;
-  const HeevdProb P = probs[blockIdx.y];
-  const int n = P.n, ell = P.ell;
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int t = blockIdx.x * 8 + wid;
-  if (t >= ell || n > NK * 32) return;
-  const R* Y = (const R*)P.Y;
-  CX z[NK];
-#pragma unroll
-  for (int k = 0; k < NK; ++k) {
-    const int r = lane + 32 * k;
-    z[k] = (r < n) ? mk<CX>(Y[(int64_t)r * ell + t], 0) : czero<CX>();
-  }
-  const CX* H = (const CX*)P.H;
-  const CX* tau = (const CX*)P.tau;
-  for (int j = n - 2; j >= 0; --j) {
-    const CX tj = tau[j];
-    if (tj.x == R(0) && tj.y == R(0)) continue;
-    const CX* row = H + (int64_t)j * P.ldh;
-    CX s = czero<CX>();
-#pragma unroll
-    for (int k = 0; k < NK; ++k) {
-      const int r = lane + 32 * k;
-      if (r >= j + 1 && r < n) {
-        const CX vr = (r == j + 1) ? mk<CX>(1, 0) : row[r];
-        cfmac(s, vr, z[k]);
-      }
-    }
-    s = warp_csum(s);
-    const CX ts = cmul(tj, s);
-#pragma unroll
-    for (int k = 0; k < NK; ++k) {
-      const int r = lane + 32 * k;
-      if (r >= j + 1 && r < n) {
-        const CX vr = (r == j + 1) ? mk<CX>(1, 0) : row[r];
-        z[k] = csub(z[k], cmul(vr, ts));
-      }
-    }
-  }
-  CX* V = (CX*)P.V;
-#pragma unroll
-  for (int k = 0; k < NK; ++k) {
-    const int r = lane + 32 * k;
-    if (r < n) V[(int64_t)r * P.ldv + t] = z[k];
-  }
-}
-
+// ------------------------------------------------------------------ stage 5 (backtransform2_kernel below)
 // ------------------------------------------------------------------ stage 6
 // GEMM problems for one Newton-Schulz step: M = Vs^H Vs; Vd = 1.5 Vs - 0.5 Vs M
 __global__ void polish_setup_kernel(const HeevdProb* __restrict__ probs, GemmProb* gp, int count,
@@ -473,6 +425,7 @@ __global__ void polish_setup_kernel(const HeevdProb* __restrict__ probs, GemmPro
   g.M = P.ell; g.N = P.ell; g.K = P.n;
   g.opA = 2; g.opB = 0;
   g.alpha_re = 1; g.alpha_im = 0; g.beta_re = 0; g.beta_im = 0;
+  if (P.skip_vectors) g.M = 0;
   gp[i] = g;
   GemmProb h;
   h.A = Vs; h.B = P.M; h.D = Vd; h.Csrc = Vs;
@@ -480,13 +433,80 @@ __global__ void polish_setup_kernel(const HeevdProb* __restrict__ probs, GemmPro
   h.M = P.n; h.N = P.ell; h.K = P.ell;
   h.opA = 0; h.opB = 0;
   h.alpha_re = -0.5; h.alpha_im = 0; h.beta_re = 1.5; h.beta_im = 0;
+  if (P.skip_vectors) h.M = 0;
   gp[count + i] = h;
+}
+
+// V = Q Y with the reflector of each step staged once per CTA in shared memory
+// (double-buffered, one barrier per reflector); each warp owns two columns of Y
+// held in registers.  WARPS warps per CTA -> 2*WARPS columns per CTA.
+template <typename CX, int NK, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) backtransform2_kernel(const HeevdProb* __restrict__ probs) {
+  typedef typename cx_traits<CX>::R R;
+  const HeevdProb P = probs[blockIdx.y];
+  const int n = P.n, ell = P.ell;
+  const int col0 = blockIdx.x * 2 * WARPS;
+  if (col0 >= ell || n > NK * 32 || P.skip_vectors) return;
+  __shared__ CX vbuf[2][NK * 32];
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int t0 = col0 + 2 * wid, t1 = t0 + 1;
+  const bool h0 = t0 < ell, h1 = t1 < ell;
+  const R* Y = (const R*)P.Y;
+  CX z0[NK], z1[NK];
+#pragma unroll
+  for (int k = 0; k < NK; ++k) {
+    const int r = lane + 32 * k;
+    z0[k] = (r < n && h0) ? mk<CX>(Y[(int64_t)r * ell + t0], 0) : czero<CX>();
+    z1[k] = (r < n && h1) ? mk<CX>(Y[(int64_t)r * ell + t1], 0) : czero<CX>();
+  }
+  const CX* H = (const CX*)P.H;
+  const CX* tau = (const CX*)P.tau;
+  for (int j = n - 2; j >= 0; --j) {
+    CX* buf = vbuf[j & 1];
+    const CX* row = H + (int64_t)j * P.ldh;
+    for (int r = tid; r < n; r += WARPS * 32)
+      buf[r] = (r <= j) ? czero<CX>() : (r == j + 1 ? mk<CX>(1, 0) : row[r]);
+    __syncthreads();
+    const CX tj = tau[j];
+    if (tj.x == R(0) && tj.y == R(0)) continue;
+    CX s0 = czero<CX>(), s1 = czero<CX>();
+#pragma unroll
+    for (int k = 0; k < NK; ++k) {
+      const int r = lane + 32 * k;
+      if (r < n) {
+        const CX vr = buf[r];
+        cfmac(s0, vr, z0[k]);
+        cfmac(s1, vr, z1[k]);
+      }
+    }
+    s0 = cmul(tj, warp_csum(s0));
+    s1 = cmul(tj, warp_csum(s1));
+#pragma unroll
+    for (int k = 0; k < NK; ++k) {
+      const int r = lane + 32 * k;
+      if (r < n) {
+        const CX vr = buf[r];
+        z0[k] = csub(z0[k], cmul(vr, s0));
+        z1[k] = csub(z1[k], cmul(vr, s1));
+      }
+    }
+  }
+  CX* V = (CX*)P.V;
+#pragma unroll
+  for (int k = 0; k < NK; ++k) {
+    const int r = lane + 32 * k;
+    if (r < n) {
+      if (h0) V[(int64_t)r * P.ldv + t0] = z0[k];
+      if (h1) V[(int64_t)r * P.ldv + t1] = z1[k];
+    }
+  }
 }
 
 template <typename CX, int NK>
 int launch_bt(const HeevdProb* probs, int count, int maxell, cudaStream_t s) {
-  dim3 grid((maxell + 7) / 8, count);
-  backtransform_kernel<CX, NK><<<grid, 256, 0, s>>>(probs);
+  constexpr int WARPS = (sizeof(CX) * NK > 128) ? 8 : 16;
+  dim3 grid((maxell + 2 * WARPS - 1) / (2 * WARPS), count);
+  backtransform2_kernel<CX, NK, WARPS><<<grid, WARPS * 32, 0, s>>>(probs);
   AGB_CHECK_LAUNCH();
   return AGB_OK;
 }
@@ -494,7 +514,7 @@ int launch_bt(const HeevdProb* probs, int count, int maxell, cudaStream_t s) {
 }  // namespace
 
 template <typename CX>
-int launch_heevd(HeevdProb* probs, GemmProb* gp, int count, int maxn, int maxell, cudaStream_t s) {
+int launch_heevd_values(HeevdProb* probs, int count, int maxn, int maxell, cudaStream_t s) {
   typedef typename cx_traits<CX>::R R;
   if (count <= 0 || maxn <= 0) return AGB_OK;
   if (maxn > 1024) return AGB_ERR_UNSUPPORTED;
@@ -505,24 +525,43 @@ int launch_heevd(HeevdProb* probs, GemmProb* gp, int count, int maxn, int maxell
     cudaFuncSetAttribute(tridiag_kernel<CX>, cudaFuncAttributeMaxDynamicSharedMemorySize, 65536);
     attr_set[esz == 16] = true;
   }
-  tridiag_kernel<CX><<<count, 1024, sm_tri, s>>>(probs);
-  AGB_CHECK_LAUNCH();
+  prof_mark(AGB_ST_TRIDIAG, s);
+  if (tridiag_cluster_size(esz, maxn) > 0) {
+    const int rc0 = launch_tridiag_cluster<CX>(probs, count, maxn, s);
+    if (rc0) return rc0;
+  } else {
+    tridiag_kernel<CX><<<count, 1024, sm_tri, s>>>(probs);
+    AGB_CHECK_LAUNCH();
+  }
   if (maxell <= 0) return AGB_OK;
   const size_t sm_r = 2 * (size_t)maxn * sizeof(R);
+  prof_mark(AGB_ST_BISECT, s);
   bisect_kernel<R><<<dim3((maxell + 7) / 8, count), 256, sm_r, s>>>(probs);
   AGB_CHECK_LAUNCH();
+  return AGB_OK;
+}
+
+template <typename CX>
+int launch_heevd_vectors(HeevdProb* probs, GemmProb* gp, int count, int maxn, int maxell, cudaStream_t s) {
+  typedef typename cx_traits<CX>::R R;
+  if (count <= 0 || maxn <= 0 || maxell <= 0) return AGB_OK;
+  const size_t sm_r = 2 * (size_t)maxn * sizeof(R);
+  prof_mark(AGB_ST_INVIT, s);
   invit_kernel<R><<<dim3((maxell + 127) / 128, count), 128, sm_r, s>>>(probs);
   AGB_CHECK_LAUNCH();
-  cluster_mgs_kernel<R><<<count, 256, (size_t)maxell * sizeof(int), s>>>(probs, 1e-4);
+  prof_mark(AGB_ST_CLUSTER, s);
+  cluster_mgs_kernel<R><<<count, 256, (size_t)maxell * sizeof(int), s>>>(probs, 1e-5);
   AGB_CHECK_LAUNCH();
   int rc;
+  prof_mark(AGB_ST_BACKTRANS, s);
   if (maxn <= 128) rc = launch_bt<CX, 4>(probs, count, maxell, s);
   else if (maxn <= 256) rc = launch_bt<CX, 8>(probs, count, maxell, s);
   else if (maxn <= 512) rc = launch_bt<CX, 16>(probs, count, maxell, s);
   else rc = launch_bt<CX, 32>(probs, count, maxell, s);
   if (rc) return rc;
-  for (int step = 0; step < 2; ++step) {
-    polish_setup_kernel<<<(count + 127) / 128, 128, 0, s>>>(probs, gp, count, step);
+  prof_mark(AGB_ST_POLISH, s);
+  for (int step = 0; step < 4; ++step) {
+    polish_setup_kernel<<<(count + 127) / 128, 128, 0, s>>>(probs, gp, count, step & 1);
     AGB_CHECK_LAUNCH();
     if ((rc = launch_gemm_probs<CX>(gp, count, maxell, maxell, s))) return rc;
     if ((rc = launch_gemm_probs<CX>(gp + count, count, maxn, maxell, s))) return rc;
@@ -530,8 +569,19 @@ int launch_heevd(HeevdProb* probs, GemmProb* gp, int count, int maxn, int maxell
   return AGB_OK;
 }
 
+template <typename CX>
+int launch_heevd(HeevdProb* probs, GemmProb* gp, int count, int maxn, int maxell, cudaStream_t s) {
+  int rc = launch_heevd_values<CX>(probs, count, maxn, maxell, s);
+  if (rc) return rc;
+  return launch_heevd_vectors<CX>(probs, gp, count, maxn, maxell, s);
+}
+
 template int launch_heevd<float2>(HeevdProb*, GemmProb*, int, int, int, cudaStream_t);
 template int launch_heevd<double2>(HeevdProb*, GemmProb*, int, int, int, cudaStream_t);
+template int launch_heevd_values<float2>(HeevdProb*, int, int, int, cudaStream_t);
+template int launch_heevd_values<double2>(HeevdProb*, int, int, int, cudaStream_t);
+template int launch_heevd_vectors<float2>(HeevdProb*, GemmProb*, int, int, int, cudaStream_t);
+template int launch_heevd_vectors<double2>(HeevdProb*, GemmProb*, int, int, int, cudaStream_t);
 
 // ------------------------------------------------------------------ standalone entry
 namespace {
@@ -548,6 +598,7 @@ __global__ void heevd_setup_kernel(HeevdProb* probs, void* H, void* evecs, char*
   p.V = (char*)evecs + (size_t)b * n * ell * esz;
   p.ldv = ell;
   p.seed = seed + 0x9E3779B97F4A7C15ull * (uint64_t)b;
+  p.skip_vectors = 0;
   heevd_assign_scratch_dev(p, scratch + (size_t)b * scratch_stride, esz);
   probs[b] = p;
 }

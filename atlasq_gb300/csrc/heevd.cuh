@@ -32,6 +32,7 @@ struct HeevdProb {
   void* M;       // CX[ell*ell] polish scratch
   void* scale;   // R[1] scale applied to H (eigenvalues of H = lam * scale)
   uint64_t seed;
+  int skip_vectors;  // set by the caller between the two phases: no eigenvectors needed
 };
 
 // Bytes of per-problem scratch (d, e, tau, lam, Y, lu, V2, M, scale) for one
@@ -62,8 +63,22 @@ AGB_HD size_t heevd_scratch_bytes(int esz, int n, int ell) {
 
 
 
+// Cluster (distributed shared memory) tridiagonalisation, tridiag_cluster.cu.
+size_t tridiag_cluster_smem(int esz, int n, int C);
+int tridiag_cluster_size(int esz, int n);
+template <typename CX>
+int launch_tridiag_cluster(const HeevdProb* probs, int count, int maxn, cudaStream_t s);
+
 // Launch all stages.  `probs` is a device array of `count` problems with
 // n <= maxn and ell <= maxell; `gemm_scratch` holds 4*count GemmProb entries.
 template <typename CX>
 int launch_heevd(HeevdProb* probs, GemmProb* gemm_scratch, int count, int maxn, int maxell,
                  cudaStream_t s);
+// The same work in two phases: eigenvalues (tridiag + bisect), then
+// eigenvectors (inverse iteration, clusters, back-transform, polish) for the
+// problems whose skip_vectors flag is 0.
+template <typename CX>
+int launch_heevd_values(HeevdProb* probs, int count, int maxn, int maxell, cudaStream_t s);
+template <typename CX>
+int launch_heevd_vectors(HeevdProb* probs, GemmProb* gemm_scratch, int count, int maxn, int maxell,
+                         cudaStream_t s);

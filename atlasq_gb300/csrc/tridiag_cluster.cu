@@ -1,0 +1,272 @@
+// Householder tridiagonalisation of a Hermitian matrix held in the distributed
+// shared memory of a thread-block cluster (sm_103a).
+//
+// One cluster of C CTAs (C = 1, 2, 4 or 8) per matrix.  CTA q owns the rows
+// r = q, q + C, q + 2C, ... and keeps their lower-triangular entries packed in
+// its shared memory, so the whole reduction runs on chip.  Step j (zhetd2
+// formulation, lower):
+//   A. every CTA publishes its entries of column j (rows > j) and a partial
+//      norm to all CTAs (DSMEM stores); cluster barrier; each CTA forms the
+//      reflector (beta, tau, v) redundantly.
+//   B. fused pass over the CTA's rows: apply the previous step's rank-2 update
+//      A -= v' w'^H + w' v'^H (columns > j) and accumulate the partial matvec
+//      A v (row-wise and, through the Hermitian symmetry, column-wise with
+//      shared-memory atomics); cluster barrier; each CTA sums the C partials
+//      (DSMEM loads), forms w = tau A v - 1/2 tau (p^H v) tau ... and updates
+//      column j+1 of its rows for the next reflector.
+// Outputs match the single-CTA kernel: d, e (real), tau (complex), reflector v_j
+// in row j of H (columns j+2 .. n-1, v_j[j+1] = 1 implicit), scale.
+#include <cooperative_groups.h>
+
+#include "heevd.cuh"
+#include "prof.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace {
+
+AGB_DEV int row_offset(int i, int q, int C) { return i * (q + 1) + C * (i * (i - 1) / 2); }
+
+template <typename CX>
+__global__ void __launch_bounds__(512, 1) tridiag_cluster_kernel(const HeevdProb* __restrict__ probs, int C) {
+  typedef typename cx_traits<CX>::R R;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int q = (int)cluster.block_rank();
+  const HeevdProb P = probs[blockIdx.x / C];
+  const int n = P.n;
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, wid = tid >> 5, nw = nt >> 5;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int nrows = (n - q + C - 1) / C;  // rows owned (q < n)
+  const int nown = (q < n) ? nrows : 0;
+  // The exchange vectors sit at the same shared-memory offset in every CTA of
+  // the cluster (map_shared_rank maps an address to the same offset in the
+  // peer CTA); the packed rows, whose size differs per CTA, come after them.
+  CX* xbuf = (CX*)smem_raw;  // column j, written remotely by the owners
+  CX* pp = xbuf + n;         // partial matvec, read remotely
+  CX* v = pp + n;
+  CX* w = v + n;
+  CX* vprev = w + n;
+  CX* wprev = vprev + n;
+  CX* rows = wprev + n;
+  __shared__ R normp[8];
+  __shared__ R red[32];
+  __shared__ CX sc[4];
+  __shared__ R mxp[8];
+  CX* H = (CX*)P.H;
+  const int64_t ld = P.ldh;
+  R* d = (R*)P.d;
+  R* e = (R*)P.e;
+  CX* tau = (CX*)P.tau;
+
+  // ---- scale by the largest diagonal magnitude
+  R mx = 0;
+  for (int i = tid; i < nown; i += nt) {
+    const int r = q + i * C;
+    mx = fmax(mx, fabs(H[(int64_t)r * ld + r].x));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if (lane == 0) red[wid] = mx;
+  __syncthreads();
+  if (tid == 0) {
+    R m = 0;
+    for (int i = 0; i < nw; ++i) m = fmax(m, red[i]);
+    for (int k = 0; k < C; ++k) *cluster.map_shared_rank(&mxp[q], k) = m;
+  }
+  cluster.sync();
+  mx = 0;
+  for (int k = 0; k < C; ++k) mx = fmax(mx, mxp[k]);
+  if (mx == R(0)) mx = R(1);
+  if (q == 0 && tid == 0) *((R*)P.scale) = mx;
+  const R inv = R(1) / mx;
+  // ---- load own rows (lower triangle, scaled)
+  for (int i = wid; i < nown; i += nw) {
+    const int r = q + i * C;
+    CX* dst = rows + row_offset(i, q, C);
+    const CX* src = H + (int64_t)r * ld;
+    for (int c = lane; c <= r; c += 32) dst[c] = cscale(src[c], inv);
+  }
+  __syncthreads();
+  if (n == 1) {
+    if (tid == 0) {
+      d[0] = rows[0].x;
+      e[0] = 0;
+      tau[0] = czero<CX>();
+    }
+    return;
+  }
+  bool prev_active = false;
+  for (int j = 0; j <= n - 2; ++j) {
+    // ---------------- A: publish column j (rows >= j+1) and the partial norm
+    if (q == (j % C) && tid == 0) d[j] = rows[row_offset(j / C, q, C) + j].x;
+    R part = 0;
+    {
+      // own rows r >= j+1: local index i >= i0
+      const int i0 = (j + 1 - q + C - 1) / C > 0 ? (j + 1 - q + C - 1) / C : 0;
+      for (int i = i0 + tid; i < nown; i += nt) {
+        const int r = q + i * C;
+        const CX x = rows[row_offset(i, q, C) + j];
+        for (int k = 0; k < C; ++k) cluster.map_shared_rank(xbuf, k)[r] = x;
+        if (r >= j + 2) part += cabs2(x);
+      }
+    }
+    part = block_sum(part, red);
+    if (tid == 0)
+      for (int k = 0; k < C; ++k) *cluster.map_shared_rank(&normp[q], k) = part;
+    cluster.sync();
+    if (tid == 0) {
+      R xn2 = 0;
+      for (int k = 0; k < C; ++k) xn2 += normp[k];
+      const CX alpha = xbuf[j + 1];
+      CX t = czero<CX>(), s = czero<CX>();
+      R beta;
+      if (xn2 == R(0) && alpha.y == R(0)) {
+        beta = alpha.x;
+      } else {
+        beta = -copysign(sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xn2), alpha.x);
+        t = mk<CX>((beta - alpha.x) / beta, -alpha.y / beta);
+        s = cinv(csub(alpha, mk<CX>(beta, 0)));
+      }
+      sc[0] = t;
+      sc[1] = s;
+      if (q == 0) {
+        e[j] = beta;
+        tau[j] = t;
+      }
+    }
+    __syncthreads();
+    const CX t = sc[0], s = sc[1];
+    const bool active = (t.x != R(0) || t.y != R(0));
+    for (int r = j + 1 + tid; r < n; r += nt) {
+      const CX vr = (r == j + 1) ? mk<CX>(1, 0) : cmul(xbuf[r], s);
+      v[r] = vr;
+      pp[r] = czero<CX>();
+      if (q == 0 && r >= j + 2) H[(int64_t)j * ld + r] = vr;  // reflector storage
+    }
+    __syncthreads();
+    // ---------------- B: fused previous update + partial matvec over own rows
+    {
+      const int i0 = (j + 1 - q + C - 1) / C > 0 ? (j + 1 - q + C - 1) / C : 0;
+      for (int i = i0 + wid; i < nown; i += nw) {
+        const int r = q + i * C;
+        CX* row = rows + row_offset(i, q, C);
+        const CX vr = vprev[r], wr = wprev[r], vjr = v[r];
+        CX acc = czero<CX>();
+        for (int c = j + 1 + lane; c <= r; c += 32) {
+          CX a = row[c];
+          if (prev_active && c >= j + 1 && j >= 1) {
+            // column j (== previous j+1) was updated at the end of the previous step
+            if (c > j) {
+              a = csub(a, cmul(vr, cconj(wprev[c])));
+              a = csub(a, cmul(wr, cconj(vprev[c])));
+              row[c] = a;
+            }
+          }
+          if (active) {
+            cfma(acc, a, v[c]);
+            if (c < r) {
+              const CX contrib = cmulc(a, vjr);  // conj(A[r][c]) * v_r
+              atomicAdd(&pp[c].x, contrib.x);
+              atomicAdd(&pp[c].y, contrib.y);
+            }
+          }
+        }
+        if (active) {
+          acc = warp_csum(acc);
+          if (lane == 0) {
+            atomicAdd(&pp[r].x, acc.x);
+            atomicAdd(&pp[r].y, acc.y);
+          }
+        }
+      }
+    }
+    cluster.sync();
+    // p = tau * sum_k pp_k ; K = -1/2 tau (p^H v) ; w = p + K v   (rows >= j+1, full length)
+    CX kpart = czero<CX>();
+    for (int r = j + 1 + tid; r < n; r += nt) {
+      CX acc = czero<CX>();
+      for (int k = 0; k < C; ++k) acc = cadd(acc, cluster.map_shared_rank(pp, k)[r]);
+      const CX pr = cmul(t, acc);
+      w[r] = pr;
+      cfmac(kpart, pr, v[r]);
+    }
+    const R kr = block_sum(kpart.x, red);
+    const R ki = block_sum(kpart.y, red);
+    const CX K = cscale(cmul(t, mk<CX>(kr, ki)), R(-0.5));
+    for (int r = j + 1 + tid; r < n; r += nt) w[r] = cadd(w[r], cmul(K, v[r]));
+    __syncthreads();
+    // update column j+1 of own rows r >= j+1 (next reflector's column)
+    if (active) {
+      const CX vc = v[j + 1], wc = w[j + 1];
+      const int i0 = (j + 1 - q + C - 1) / C > 0 ? (j + 1 - q + C - 1) / C : 0;
+      for (int i = i0 + tid; i < nown; i += nt) {
+        const int r = q + i * C;
+        CX* a = rows + row_offset(i, q, C) + (j + 1);
+        CX val = *a;
+        val = csub(val, cmul(v[r], cconj(wc)));
+        val = csub(val, cmul(w[r], cconj(vc)));
+        *a = val;
+      }
+    }
+    // keep (v, w) for the fused update of the next step (columns >= j+2)
+    for (int r = j + 1 + tid; r < n; r += nt) {
+      vprev[r] = v[r];
+      wprev[r] = w[r];
+    }
+    prev_active = active;
+    __syncthreads();
+  }
+  if (q == ((n - 1) % C) && tid == 0) {
+    d[n - 1] = rows[row_offset((n - 1) / C, q, C) + (n - 1)].x;
+    e[n - 1] = 0;
+  }
+  cluster.sync();  // keep every CTA's shared memory alive until remote readers finish
+}
+
+}  // namespace
+
+// Shared memory bytes for cluster size C and matrix size n.
+size_t tridiag_cluster_smem(int esz, int n, int C) {
+  size_t best = 0;
+  for (int q = 0; q < C && q < n; ++q) {
+    const int nown = (n - q + C - 1) / C;
+    const size_t elems = (size_t)nown * (q + 1) + (size_t)C * ((size_t)nown * (nown - 1) / 2);
+    if (elems > best) best = elems;
+  }
+  return (best + 6 * (size_t)n) * esz;
+}
+
+// Pick the smallest power-of-two cluster whose shared memory fits; 0 if none.
+int tridiag_cluster_size(int esz, int n) {
+  for (int C = 1; C <= 8; C *= 2)
+    if (tridiag_cluster_smem(esz, n, C) <= 200 * 1024) return C;
+  return 0;
+}
+
+template <typename CX>
+int launch_tridiag_cluster(const HeevdProb* probs, int count, int maxn, cudaStream_t s) {
+  const int esz = sizeof(CX);
+  const int C = tridiag_cluster_size(esz, maxn);
+  if (C == 0) return AGB_ERR_UNSUPPORTED;
+  const size_t smem = tridiag_cluster_smem(esz, maxn, C);
+  cudaFuncSetAttribute(tridiag_cluster_kernel<CX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(count * C, 1, 1);
+  cfg.blockDim = dim3(512, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = C;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaError_t err = cudaLaunchKernelEx(&cfg, tridiag_cluster_kernel<CX>, probs, C);
+  agb_note_launch();
+  if (err != cudaSuccess) return AGB_ERR_CUDA;
+  return AGB_OK;
+}
+
+template int launch_tridiag_cluster<float2>(const HeevdProb*, int, int, cudaStream_t);
+template int launch_tridiag_cluster<double2>(const HeevdProb*, int, int, cudaStream_t);

@@ -13,6 +13,7 @@
 #include <math.h>
 
 #include "heevd.cuh"
+#include "prof.cuh"
 
 namespace {
 
@@ -87,6 +88,7 @@ __global__ void setup_kernel(const int64_t* __restrict__ desc, int ng, char* ws,
   p.V = slab + L.V;
   p.ldv = ell;
   p.seed = (uint64_t)D[AGB_D_SEED];
+  p.skip_vectors = 0;
   heevd_assign_scratch_dev(p, slab + L.heevd, esz);
   hp[g] = p;
   // gp[0..2ng) reserved for the eigensolver polish; [2ng, 3ng) Gram; [3ng, 4ng) AV
@@ -180,6 +182,146 @@ __global__ void __launch_bounds__(256) contract_gate_kernel(const ContractProb* 
     }
 }
 
+// The reference rank rule (truncation.py:21-83) on sigma^2 values sorted
+// descending, with torch-CPU float32 semantics when f32 (double-accumulated
+// cumsum rounded to float32 per element; threshold f32(f32(1 - eps^2) * total)).
+// total is E[-1] of the reference: our own cumsum end when every potentially
+// non-zero value is present (ell >= kmax), else ||X||_F^2.
+AGB_DEV void rank_rule(const double* s_sorted, int ell, int kmax, int cap, double eps, bool f32,
+                       double total_d, int& k, double& eps_local, double& entropy, double& condS,
+                       int& status, int& needed) {
+  eps_local = 0;
+  entropy = 0;
+  condS = INFINITY;
+  status = AGB_OK;
+  needed = ell;
+  if (ell == 0) {
+    k = 0;
+    return;
+  }
+  double total;
+  if (ell >= kmax) {
+    double a = 0;
+    for (int t = 0; t < ell; ++t) {
+      if (f32) {
+        const float s = sqrtf((float)s_sorted[t]);
+        a += (double)(s * s);
+      } else {
+        const double s = sqrt(s_sorted[t]);
+        a += s * s;
+      }
+    }
+    total = f32 ? (double)(float)a : a;
+  } else {
+    total = f32 ? (double)(float)total_d : total_d;
+  }
+  if (total < 1e-30) {
+    k = 1;
+    return;
+  }
+  double thresh;
+  if (f32) thresh = (double)(float)((float)(1.0 - eps * eps) * (float)total);
+  else thresh = (1.0 - eps * eps) * total;
+  double acc = 0;
+  int ktol = -1;
+  for (int t = 0; t < ell; ++t) {
+    double sq;
+    if (f32) {
+      const float sv = sqrtf((float)s_sorted[t]);
+      sq = (double)(sv * sv);
+    } else {
+      const double sv = sqrt(s_sorted[t]);
+      sq = sv * sv;
+    }
+    acc += sq;
+    const double Et = f32 ? (double)(float)acc : acc;
+    if (Et >= thresh) {
+      ktol = t + 1;
+      break;
+    }
+  }
+  const int full = min(kmax, cap);
+  if (ktol < 0) {
+    if (ell < full) {
+      status = AGB_ERR_RANK;
+      needed = full;
+      ktol = ell;
+    } else {
+      ktol = kmax;
+    }
+  }
+  ktol = min(ktol, kmax);
+  k = min(ktol, cap);
+  k = min(k, ell);
+  acc = 0;
+  for (int t = 0; t < k; ++t) {
+    if (f32) {
+      const float sv = sqrtf((float)s_sorted[t]);
+      acc += (double)(sv * sv);
+    } else {
+      const double sv = sqrt(s_sorted[t]);
+      acc += sv * sv;
+    }
+  }
+  const double Ek = f32 ? (double)(float)acc : acc;
+  const double rem = total - Ek;
+  eps_local = f32 ? (double)sqrtf((float)fmax(rem, 0.0)) : sqrt(fmax(rem, 0.0));
+  double ssum = 0;
+  for (int t = 0; t < k; ++t) ssum += s_sorted[t];
+  for (int t = 0; t < k; ++t) {
+    const double p = s_sorted[t] / ssum;
+    entropy -= p * log(fmax(p, 1e-30));
+  }
+  if (k > 1) {
+    if (f32) {
+      const float s0 = sqrtf((float)s_sorted[0]), sk = sqrtf((float)s_sorted[k - 1]);
+      condS = sk > 0.f ? (double)(s0 / sk) : INFINITY;
+    } else {
+      const double s0 = sqrt(s_sorted[0]), sk = sqrt(s_sorted[k - 1]);
+      condS = sk > 0 ? s0 / sk : INFINITY;
+    }
+  }
+}
+
+// Between the eigenvalue and eigenvector phases: when the rank rule keeps
+// every column (k == n <= m), any orthonormal basis factorises X exactly
+// (X = (X V)(V^H)), so the gate takes V = I: A_new = X, B_new = I.  This is a
+// unitary gauge change on the bond relative to the SVD factors, so the state
+// and every later gate's spectrum are unchanged.  Flat spectra (maximally
+// mixed small subsystems at the chain ends) would otherwise need one large
+// eigenvalue cluster orthogonalised.
+template <typename CX>
+__global__ void prerank_kernel(int64_t* __restrict__ desc, int ng, char* ws) {
+  typedef typename cx_traits<CX>::R R;
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= ng) return;
+  int64_t* D = desc + (int64_t)g * AGB_D_NFIELDS;
+  const int chiL = (int)D[AGB_D_CHIL], chiR = (int)D[AGB_D_CHIR];
+  const int m = 2 * chiL, n = 2 * chiR, ell = (int)D[AGB_D_ELL], cap = (int)D[AGB_D_CAP];
+  HeevdProb* hp = (HeevdProb*)ws;
+  GemmProb* gp = (GemmProb*)(ws + agb_align((size_t)ng * sizeof(HeevdProb)));
+  D[AGB_D_MODE] = 0;
+  hp[g].skip_vectors = 0;
+  if (m < n || ell != n || n > 1024) return;
+  const HeevdProb P = hp[g];
+  const R* lam = (const R*)P.lam;
+  const R scale = *((const R*)P.scale);
+  double s2[1024];
+  for (int t = 0; t < ell; ++t) {
+    const R v = lam[t] * scale;
+    const double a = v > R(0) ? (double)v : 0.0;
+    s2[t] = (sizeof(R) == 4) ? (double)(float)a : a;
+  }
+  int k, status, needed;
+  double el, en, cs;
+  rank_rule(s2, ell, min(m, n), cap, dbits(D[AGB_D_EPS]), sizeof(R) == 4, 0.0, k, el, en, cs, status, needed);
+  if (status == AGB_OK && k == n) {
+    D[AGB_D_MODE] = 1;
+    hp[g].skip_vectors = 1;
+    gp[3 * ng + g].M = 0;  // no X*V product
+  }
+}
+
 // ------------------------------------------------------------------ rank selection
 // One block per gate.  sigma_t^2 = ||AV[:, t]||^2, sorted descending; then the
 // reference rank rule with torch-CPU float32 semantics for complex64:
@@ -209,18 +351,39 @@ __global__ void __launch_bounds__(1024) rank_kernel(int64_t* __restrict__ desc, 
   double part = 0;
   for (int64_t i = tid; i < (int64_t)m * n; i += nt) part += (double)cabs2(X[i]);
   const double total_d = block_sum(part, red);
+  __shared__ int nonfinite;
+  if (tid == 0) nonfinite = !isfinite(total_d);
+  __syncthreads();
+  const int mode0 = (int)D[AGB_D_MODE];
+  const HeevdProb* hp = (const HeevdProb*)ws;
   for (int t = tid; t < ell; t += nt) {
     double acc = 0;
-    for (int r = 0; r < m; ++r) acc += (double)cabs2(AV[(int64_t)r * ell + t]);
+    if (mode0 == 1) {
+      // identity basis: the eigenvalues (descending) are the sigma^2
+      const R v = ((const R*)hp[g].lam)[t] * *((const R*)hp[g].scale);
+      acc = v > R(0) ? (double)v : 0.0;
+    } else {
+      for (int r = 0; r < m; ++r) acc += (double)cabs2(AV[(int64_t)r * ell + t]);
+    }
+    if (!isfinite(acc)) {
+      nonfinite = 1;
+      acc = -1.0;  // sorts last; the gate is reported as failed below
+    }
     s_raw[t] = f32 ? (double)(float)acc : acc;
   }
   __syncthreads();
+  // rank of each value (descending, ties by index): always a permutation of 0..ell-1.
+  // The identity-basis mode keeps the eigenvalue order (already descending), so
+  // the rank rule sees exactly the values the pre-rank decision used.
   for (int t = tid; t < ell; t += nt) {
     const double v = s_raw[t];
-    int rk = 0;
-    for (int u = 0; u < ell; ++u) {
-      const double w = s_raw[u];
-      rk += (w > v) || (w == v && u < t);
+    int rk = t;
+    if (mode0 != 1) {
+      rk = 0;
+      for (int u = 0; u < ell; ++u) {
+        const double w = s_raw[u];
+        rk += (w > v) || (w == v && u < t);
+      }
     }
     s_sorted[rk] = v;
     perm[rk] = t;
@@ -229,103 +392,14 @@ __global__ void __launch_bounds__(1024) rank_kernel(int64_t* __restrict__ desc, 
   for (int t = tid; t < ell; t += nt) sig2[t] = s_sorted[t];
   if (tid != 0) return;
   const int kmax = min(m, n);
-  int k;
-  double eps_local = 0, entropy = 0, condS = INFINITY;
-  int status = AGB_OK, needed = ell;
-  // singular values as the reference sees them: S = sqrt(sigma^2) in working precision
-  if (ell == 0) {
+  int k, status, needed;
+  double eps_local, entropy, condS;
+  const int mode = (int)D[AGB_D_MODE];
+  rank_rule(s_sorted, ell, kmax, cap, eps, f32, total_d, k, eps_local, entropy, condS, status, needed);
+  (void)mode;
+  if (nonfinite) {
+    status = AGB_ERR_NOCONV;
     k = 0;
-  } else {
-    // total = E[-1] of the reference: when every potentially non-zero pair was
-    // computed (ell == min(m, n)) it is the end of our own cumsum; otherwise the
-    // Frobenius norm of X stands in for the unseen tail.
-    double total;
-    if (ell >= kmax) {
-      double a = 0;
-      for (int t = 0; t < ell; ++t) {
-        if (f32) {
-          const float s = sqrtf((float)s_sorted[t]);
-          a += (double)(s * s);
-        } else {
-          const double s = sqrt(s_sorted[t]);
-          a += s * s;
-        }
-      }
-      total = f32 ? (double)(float)a : a;
-    } else {
-      total = f32 ? (double)(float)total_d : total_d;
-    }
-    if (total < 1e-30) {
-      k = 1;
-      eps_local = 0;
-      entropy = 0;
-      condS = INFINITY;
-    } else {
-      double thresh;
-      if (f32) thresh = (double)(float)((float)(1.0 - eps * eps) * (float)total);
-      else thresh = (1.0 - eps * eps) * total;
-      double acc = 0;
-      int ktol = -1;
-      double Ek = 0;
-      for (int t = 0; t < ell; ++t) {
-        double sq;
-        if (f32) {
-          const float s = sqrtf((float)s_sorted[t]);
-          sq = (double)(s * s);
-        } else {
-          const double s = sqrt(s_sorted[t]);
-          sq = s * s;
-        }
-        acc += sq;
-        const double Et = f32 ? (double)(float)acc : acc;
-        if (Et >= thresh) {
-          ktol = t + 1;
-          break;
-        }
-      }
-      const int full = min(kmax, cap);
-      if (ktol < 0) {
-        if (ell < full) {
-          status = AGB_ERR_RANK;
-          needed = full;
-          ktol = ell;
-        } else {
-          ktol = kmax;
-        }
-      }
-      ktol = min(ktol, kmax);
-      k = min(ktol, cap);
-      k = min(k, ell);
-      // E[k-1]
-      acc = 0;
-      for (int t = 0; t < k; ++t) {
-        if (f32) {
-          const float s = sqrtf((float)s_sorted[t]);
-          acc += (double)(s * s);
-        } else {
-          const double s = sqrt(s_sorted[t]);
-          acc += s * s;
-        }
-      }
-      Ek = f32 ? (double)(float)acc : acc;
-      const double rem = total - Ek;
-      eps_local = f32 ? (double)sqrtf((float)fmax(rem, 0.0)) : sqrt(fmax(rem, 0.0));
-      double ssum = 0;
-      for (int t = 0; t < k; ++t) ssum += s_sorted[t];
-      for (int t = 0; t < k; ++t) {
-        const double p = s_sorted[t] / ssum;
-        entropy -= p * log(fmax(p, 1e-30));
-      }
-      if (k > 1) {
-        if (f32) {
-          const float s0 = sqrtf((float)s_sorted[0]), sk = sqrtf((float)s_sorted[k - 1]);
-          condS = sk > 0.f ? (double)(s0 / sk) : INFINITY;
-        } else {
-          const double s0 = sqrt(s_sorted[0]), sk = sqrt(s_sorted[k - 1]);
-          condS = sk > 0 ? s0 / sk : INFINITY;
-        }
-      }
-    }
   }
   D[AGB_D_K] = k;
   D[AGB_D_EPSLOC] = bitsd(eps_local);
@@ -347,19 +421,34 @@ __global__ void scatter_kernel(const int64_t* __restrict__ desc, char* ws) {
   const Slab Ls = slab_layout(m, n, ell, sizeof(CX));
   const CX* AV = (const CX*)(slab + Ls.AV);
   const CX* V = (const CX*)(slab + Ls.V);
+  const CX* X = (const CX*)(slab + Ls.X);
   const int* perm = (const int*)(slab + Ls.perm);
+  const int mode = (int)D[AGB_D_MODE];
   CX* An = (CX*)D[AGB_D_ANEW];
   CX* Bn = (CX*)D[AGB_D_BNEW];
+  if (!An || !Bn || k <= 0 || k > ell) return;
+  if (mode == 1 && k != n) return;
   const int64_t na = (int64_t)m * k, nb = (int64_t)k * n;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < na + nb;
        i += (int64_t)gridDim.x * blockDim.x) {
+    if (mode == 1) {
+      if (i < na) {
+        An[i] = X[i];  // k == n: A_new = X
+      } else {
+        const int64_t ii = i - na;
+        Bn[ii] = ((ii / n) == (ii % n)) ? mk<CX>(1, 0) : czero<CX>();
+      }
+      continue;
+    }
     if (i < na) {
       const int r = (int)(i / k), j = (int)(i % k);
-      An[i] = AV[(int64_t)r * ell + perm[j]];
+      const int pj = perm[j];
+      An[i] = (pj >= 0 && pj < ell) ? AV[(int64_t)r * ell + pj] : czero<CX>();
     } else {
       const int64_t ii = i - na;
       const int j = (int)(ii / n), c = (int)(ii % n);
-      Bn[ii] = cconj(V[(int64_t)c * ell + perm[j]]);
+      const int pj = perm[j];
+      Bn[ii] = (pj >= 0 && pj < ell) ? cconj(V[(int64_t)c * ell + pj]) : czero<CX>();
     }
   }
 }
@@ -367,6 +456,7 @@ __global__ void scatter_kernel(const int64_t* __restrict__ desc, char* ws) {
 template <typename CX>
 int run_impl(int ng, int64_t* desc, int maxL, int maxM, int maxR, int maxell, char* ws, cudaStream_t s) {
   const int esz = sizeof(CX);
+  prof_mark(AGB_ST_SETUP, s);
   setup_kernel<<<(ng + 127) / 128, 128, 0, s>>>(desc, ng, ws, esz);
   AGB_CHECK_LAUNCH();
   HeevdProb* hp = (HeevdProb*)ws;
@@ -374,17 +464,26 @@ int run_impl(int ng, int64_t* desc, int maxL, int maxM, int maxR, int maxell, ch
   ContractProb* cp = (ContractProb*)(ws + agb_align((size_t)ng * sizeof(HeevdProb)) +
                                      agb_align((size_t)ng * 4 * sizeof(GemmProb)));
   ContractProb none = {};
+  prof_mark(AGB_ST_CONTRACT, s);
   contract_gate_kernel<CX><<<dim3((maxR + 15) / 16, (maxL + 15) / 16, ng), 256, 0, s>>>(cp, none);
   AGB_CHECK_LAUNCH();
   const int maxm = 2 * maxL, maxn = 2 * maxR;
+  prof_mark(AGB_ST_GRAM, s);
   int rc = launch_gemm_probs<CX>(gp + 2 * ng, ng, maxn, maxn, s);
   if (rc) return rc;
-  rc = launch_heevd<CX>(hp, gp, ng, maxn, maxell, s);
+  rc = launch_heevd_values<CX>(hp, ng, maxn, maxell, s);
   if (rc) return rc;
+  prerank_kernel<CX><<<(ng + 127) / 128, 128, 0, s>>>(desc, ng, ws);
+  AGB_CHECK_LAUNCH();
+  rc = launch_heevd_vectors<CX>(hp, gp, ng, maxn, maxell, s);
+  if (rc) return rc;
+  prof_mark(AGB_ST_AV, s);
   rc = launch_gemm_probs<CX>(gp + 3 * ng, ng, maxm, maxell, s);
   if (rc) return rc;
+  prof_mark(AGB_ST_RANK, s);
   rank_kernel<CX><<<ng, 1024, 2 * (size_t)maxell * sizeof(double), s>>>(desc, ng, ws);
   AGB_CHECK_LAUNCH();
+  prof_mark(AGB_ST_GAP, s);
   return AGB_OK;
 }
 
@@ -462,8 +561,10 @@ extern "C" int agb_two_site_finalize(int dtype, int ng, const int64_t* desc_dev,
   if (blocks < 1) blocks = 1;
   if (blocks > 4096) blocks = 4096;
   cudaStream_t s = (cudaStream_t)stream;
+  prof_mark(AGB_ST_SCATTER, s);
   if (dtype == AGB_C64) scatter_kernel<float2><<<dim3(blocks, ng), 256, 0, s>>>(desc_dev, (char*)ws);
   else scatter_kernel<double2><<<dim3(blocks, ng), 256, 0, s>>>(desc_dev, (char*)ws);
   AGB_CHECK_LAUNCH();
+  prof_mark(AGB_ST_GAP, s);
   return AGB_OK;
 }

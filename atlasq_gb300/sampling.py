@@ -38,6 +38,7 @@ def sample_tensors(tensors, num_shots, seed, chunk=16384, return_pz=False):
         ns = min(chunk, num_shots - c0)
         L = torch.ones(ns, 1, dtype=dt, device=dev)
         for i, T in enumerate(tensors):
+            T = T.contiguous()
             l, _, r = T.shape
             temp = ops.cgemm(L, T.reshape(l, 2 * r))
             Lnew = torch.empty(ns, r, dtype=dt, device=dev) if i < n - 1 else None

@@ -1,0 +1,406 @@
+#!/usr/bin/env python
+"""Benchmark: two-site gates/s at chi=256 (40-qubit Haar brickwork, depth 20).
+
+Workload (one "step"): the full 390-gate circuit from |0...0>, 40 qubits,
+brickwork of Haar-random 4x4 unitaries (seeded QR of complex Gaussians), chi_max
+256, eps_bond 1e-8, complex64 -- run through the AdaptiveMPS API of this package.
+
+Lines printed (rank 0, one JSON object):
+  value    gates/s with gate matrices already resident in HBM (device events)
+  e2e      gates/s through the public API with the gates in pinned host memory
+           (host->device copies and the device->host result read inside the timing)
+  roofline the dominant kernel, from the library's live per-stage CUDA events
+  cpu_baseline  the CPU oracle port (NumPy complex64 restatement of the
+           reference AdaptiveMPS) on this host, bounded sample
+  plain_gpu     the reference call sequence on this GPU with torch complex64
+           contraction + torch.linalg.svd (cuSOLVER), for the plain-form comparison
+
+``--impl reference`` times the CPU port of the reference path instead.
+Multi-GPU (torchrun): independent replicas per rank, no collective on the data
+path ("scaling": "weak").
+"""
+import argparse
+import ctypes
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+import torch
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_QUBITS, DEPTH, CHI, EPS, SEED = 40, 20, 256, 1e-8, 1234
+METRIC = "2-site gates/s at chi=256 (40q Haar brickwork depth 20, eps 1e-8)"
+WORKLOAD = "40-qubit Haar brickwork depth 20 (390 two-site gates), chi_max=256, eps_bond=1e-8, complex64"
+L2_BYTES = 129 * 1024 * 1024
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), float(p["bf16_tflops"]), "measured"
+    except Exception:
+        return 6800.0, 1900.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (SM clock, throttle reasons)."""
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 8:
+                self.samples.append(parts)
+
+    def stop(self):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        if self.thread is not None:
+            self.thread.join(timeout=2)
+        sm = []
+        mx = None
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for p in self.samples:
+            try:
+                sm.append(float(p[0]))
+                mx = float(p[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_circuit():
+    from atlasq_gb300.circuits import haar_brickwork
+    return haar_brickwork(N_QUBITS, DEPTH, seed=SEED)
+
+
+def run_ours(ops, device, dtype=torch.complex64):
+    import atlasq_gb300 as aq
+    pol = aq.DTypePolicy(default=dtype)
+    m = aq.AdaptiveMPS(N_QUBITS, bond_dim=1, eps_bond=EPS, chi_max_per_bond=CHI, device=device,
+                       dtype=dtype, dtype_policy=pol)
+    for _, q, U in ops:
+        m.apply_two_site_gate(q, U)
+    m.flush()
+    return m
+
+
+def mps_overlap(ta, tb):
+    """<a|b> with the package GEMMs (left environment sweep)."""
+    from atlasq_gb300 import ops as o
+    E = torch.ones(1, 1, dtype=torch.complex128, device=ta[0].device)
+    for A, B in zip(ta, tb):
+        A = A.to(torch.complex128).contiguous()
+        B = B.to(torch.complex128).contiguous()
+        la, _, ra = A.shape
+        lb, _, rb = B.shape
+        M = o.cgemm(E, B.reshape(lb, 2 * rb))                     # [la, 2rb]
+        E = o.cgemm(A.reshape(2 * la, ra), M.reshape(2 * la, rb), opA="C", opB="N")
+    return complex(E[0, 0].item())
+
+
+def plain_gpu_circuit(ops, device):
+    """Reference call sequence (adaptive_mps.py:182-308) with torch on the GPU:
+    einsum contraction (mps_complex.py:343-368), torch.linalg.svd (cuSOLVER),
+    the rank rule with its host syncs (truncation.py:21-83), U*S | Vh split."""
+    from atlasq_gb300.truncation import choose_rank_from_sigma
+    tensors = [torch.zeros(1, 2, 1, dtype=torch.complex64, device=device) for _ in range(N_QUBITS)]
+    for t in tensors:
+        t[0, 0, 0] = 1
+    for _, i, U in ops:
+        A, B = tensors[i], tensors[i + 1]
+        li, ri, rj = A.shape[0], A.shape[2], B.shape[2]
+        psi = torch.einsum("lpr,rqj->lpqj", A, B).permute(1, 2, 0, 3).reshape(4, li * rj)
+        X = (U @ psi).reshape(2, 2, li, rj).permute(2, 0, 1, 3).reshape(li * 2, 2 * rj)
+        Uu, S, Vh = torch.linalg.svd(X, full_matrices=False)
+        E = (S * S).cumsum(0)
+        total = E[-1]
+        thresh = (1.0 - EPS ** 2) * total
+        k = min(int(torch.searchsorted(E, thresh).item()) + 1, S.numel(), CHI)
+        _ = float(torch.sqrt(torch.clamp(total - E[k - 1], min=0)).item())
+        tensors[i] = (Uu[:, :k] * S[:k]).reshape(li, 2, k)
+        tensors[i + 1] = Vh[:k].reshape(k, 2, rj)
+    return tensors
+
+
+def cpu_port_circuit(ops, time_cap=None):
+    """CPU oracle port (NumPy complex64) over the circuit; returns gates done, seconds."""
+    from oracle import mps_oracle as mo
+    m = mo.OracleMPS(N_QUBITS, bond_dim=1, eps_bond=EPS, chi_max_per_bond=CHI, dtype=np.complex64)
+    t0 = time.perf_counter()
+    done = 0
+    for _, q, U in ops:
+        m.apply_two_site_gate(q, U.numpy())
+        done += 1
+        if time_cap is not None and time.perf_counter() - t0 > time_cap:
+            break
+    return done, time.perf_counter() - t0
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        dist.init_process_group(backend=backend)
+        return dist, ws, rank, local
+    return None, 1, 0, local
+
+
+def barrier(dist, device=None):
+    if dist is not None:
+        if device is not None and dist.get_backend() == "nccl":
+            dist.barrier(device_ids=[device.index])
+        else:
+            dist.barrier()
+
+
+def max_over_ranks(dist, x, device):
+    if dist is None:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device=device if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def reference_arm(args, dist, ws, rank):
+    """--impl reference: the reference path's CPU implementation (oracle port) on host cores."""
+    if rank != 0:
+        return
+    ops = make_circuit()
+    cores = os.cpu_count() or 1
+    cap = float(os.environ.get("AGB_REF_STEP_CAP_S", "45"))
+    for _ in range(min(args.warmup, 1)):
+        cpu_port_circuit(ops[:40])
+    total_g, total_t = 0, 0.0
+    for _ in range(args.steps):
+        g, t = cpu_port_circuit(ops, time_cap=cap)
+        total_g += g
+        total_t += t
+    v = total_g / total_t
+    sample = ("full 390-gate circuit per step" if total_g == 390 * args.steps else
+              f"{total_g} gates over {args.steps} steps (each step capped at {cap:.0f} s)")
+    line = {"metric": METRIC, "value": v, "unit": "gates/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * total_t / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "complex64", "data": "synthetic",
+            "impl": "reference", "config": {"workload": WORKLOAD, "parallelism": "replicas"},
+            "cpu_baseline": {"value": v, "unit": "gates/s", "cores": cores, "kind": "port",
+                             "sample": sample + "; NumPy complex64 restatement of AdaptiveMPS"},
+            "e2e": {"value": v, "unit": "gates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--fp64-check", action="store_true", help="also run the complex128 GPU path and report fidelity")
+    args = ap.parse_args()
+
+    dist, ws, rank, local = dist_init()
+    if args.impl == "reference":
+        reference_arm(args, dist, ws, rank)
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+
+    import atlasq_gb300 as aq
+    from atlasq_gb300 import _lib
+    lib = _lib.load()
+    device = torch.device("cuda", local)
+    torch.cuda.set_device(device)
+    ops_host = make_circuit()
+    ngates = len(ops_host)
+    ops_dev = [(k, q, U.to(device)) for k, q, U in ops_host]
+    ops_pinned = [(k, q, U.pin_memory()) for k, q, U in ops_host]
+    flush_buf = torch.empty(2 * L2_BYTES, dtype=torch.uint8, device=device)
+
+    for _ in range(max(args.warmup, 3) if args.warmup > 0 else 0):
+        run_ours(ops_dev, device)
+    torch.cuda.synchronize()
+
+    # ---------------------------------------------------------------- timed region (value)
+    lib.agb_prof_begin(200000)
+    launches0 = lib.agb_launch_count()
+    sampler = ClockSampler(local)
+    sampler.start()
+    barrier(dist, device)
+    torch.cuda.synchronize()
+    total_ms = 0.0
+    last = None
+    for _ in range(args.steps):
+        flush_buf.zero_()  # L2 flush between timed iterations (untimed)
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        last = run_ours(ops_dev, device)
+        e.record()
+        e.synchronize()
+        total_ms += s.elapsed_time(e)
+    torch.cuda.synchronize()
+    barrier(dist, device)
+    clocks = sampler.stop()
+    launches = lib.agb_launch_count() - launches0
+    ms_st = (ctypes.c_double * 16)()
+    cnt_st = (ctypes.c_int * 16)()
+    _lib.check(lib.agb_prof_end(ms_st, cnt_st, 16), "prof_end")
+    stage_ms = {name: ms_st[i] / args.steps for i, name in enumerate(_lib.STAGES)}
+    total_ms = max_over_ranks(dist, total_ms, device)
+    ms_per_step = total_ms / args.steps
+    value = ngates * ws / (ms_per_step / 1000.0)
+
+    # ---------------------------------------------------------------- e2e (host buffers)
+    torch.cuda.synchronize()
+    e2e_ms = 0.0
+    for _ in range(args.steps):
+        flush_buf.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        m = run_ours(ops_pinned, device)
+        res = m._tensors[-1].cpu()  # device->host read of the step's result
+        torch.cuda.synchronize()
+        e2e_ms += (time.perf_counter() - t0) * 1000.0
+    e2e_ms = max_over_ranks(dist, e2e_ms, device) / args.steps
+    # per step: gate matrices (16 complex64) + two descriptor uploads per gate (32 int64 each);
+    # back: one descriptor read per gate + the final site tensor
+    h2d = ngates * 16 * 8 + ngates * 2 * 32 * 8
+    d2h = ngates * 32 * 8 + res.numel() * res.element_size()
+    e2e = {"value": ngates * ws / (e2e_ms / 1000.0), "unit": "gates/s", "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": d2h}
+
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+
+    # ---------------------------------------------------------------- roofline of the dominant kernel
+    hbm, bf16, src = peaks()
+    kernels = {k: v for k, v in stage_ms.items() if k != "host_gap"}
+    dom = max(kernels, key=kernels.get)
+    # algorithmic work of each stage per step (sizes from the step's own statistics:
+    # gate on bond q has X of (2 chiL) x (2 chiR) with chiL = bond q-1, chiR = bond q+1)
+    work = {}
+    bd = last.statistics.logs
+    sizes = []
+    tl = [1] * (N_QUBITS - 1)
+    for (_, q, _), k in zip(ops_host, bd["k_star"]):
+        chiL = 1 if q == 0 else tl[q - 1]
+        chiR = 1 if q == N_QUBITS - 2 else tl[q + 1]
+        sizes.append((2 * chiL, 2 * chiR, k))
+        tl[q] = k
+    for m_, n_, k in sizes:
+        fl_tri = 16.0 / 3.0 * n_ ** 3
+        by_tri = 2.0 * n_ * n_ * 8
+        work.setdefault("tridiag", [0.0, 0.0])
+        work["tridiag"][0] += by_tri
+        work["tridiag"][1] += fl_tri
+        work.setdefault("gram", [0.0, 0.0])
+        work["gram"][0] += (m_ * n_ + n_ * n_) * 8
+        work["gram"][1] += 8.0 * m_ * n_ * n_
+        work.setdefault("xv", [0.0, 0.0])
+        work["xv"][0] += (m_ * n_ + n_ * k + m_ * k) * 8
+        work["xv"][1] += 8.0 * m_ * n_ * k
+        work.setdefault("backtransform", [0.0, 0.0])
+        work["backtransform"][0] += (n_ * n_ + 2 * n_ * k) * 8
+        work["backtransform"][1] += 8.0 * n_ * n_ * k
+    wb, wf = work.get(dom, [0.0, 0.0])
+    t_dom = stage_ms[dom] / 1000.0
+    bound = "tensor" if dom in ("gram", "xv") else "hbm"
+    if bound == "hbm":
+        achieved = wb / t_dom / 1e9 if t_dom > 0 else 0.0
+        roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "traffic": None}
+    else:
+        achieved = wf / t_dom / 1e12 if t_dom > 0 else 0.0
+        roof = {"bound": "tensor", "achieved": achieved, "peak": bf16, "unit": "TFLOP/s",
+                "frac": achieved / bf16, "traffic": None}
+    roof.update({"kernel": dom, "peak_source": src, "stage_ms_per_step": {k: round(v, 3) for k, v in stage_ms.items()},
+                 "algorithmic_flops_per_step": wf, "algorithmic_bytes_per_step": wb})
+
+    line = {"metric": METRIC, "value": value, "unit": "gates/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "complex64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "gates_per_step": ngates, "parallelism": f"replicas x{ws}",
+                       "l2": "flushed between timed steps (2x L2 write)", "precision": "fp32 SIMT + fp32 eigensolver"},
+            "clocks": clocks, "gpu_launches": launches, "e2e": e2e, "roofline": roof}
+
+    # ---------------------------------------------------------------- plain form on the same GPU
+    if not args.no_plain:
+        plain_gpu_circuit(ops_dev[:60], device)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        pt = plain_gpu_circuit(ops_dev, device)
+        torch.cuda.synchronize()
+        tp = time.perf_counter() - t0
+        f = mps_overlap([t for t in last.tensors], pt)
+        fa = mps_overlap(last.tensors, last.tensors).real
+        fb = mps_overlap(pt, pt).real
+        line["plain_gpu"] = {"value": ngates / tp, "unit": "gates/s",
+                             "what": "reference call sequence on this GPU: torch complex64 einsum + torch.linalg.svd (cuSOLVER) + host rank rule",
+                             "fidelity_vs_ours": abs(f) ** 2 / (fa * fb)}
+    if args.fp64_check:
+        t0 = time.perf_counter()
+        m64 = run_ours(ops_dev, device, dtype=torch.complex128)
+        torch.cuda.synchronize()
+        f = mps_overlap(last.tensors, m64.tensors)
+        fa = mps_overlap(last.tensors, last.tensors).real
+        fb = mps_overlap(m64.tensors, m64.tensors).real
+        line["fidelity_vs_fp64"] = {"value": abs(f) ** 2 / (fa * fb), "fp64_gpu_seconds": time.perf_counter() - t0}
+
+    # ---------------------------------------------------------------- CPU baseline (oracle port)
+    if not args.no_cpu_baseline:
+        cap = float(os.environ.get("AGB_CPU_BASELINE_CAP_S", "30"))
+        g, t = cpu_port_circuit(ops_host, time_cap=cap)
+        line["cpu_baseline"] = {"value": g / t, "unit": "gates/s", "cores": os.cpu_count() or 1, "kind": "port",
+                                "sample": (f"first {g} of 390 gates in circuit order (capped at {cap:.0f} s)"
+                                           if g < ngates else "full 390-gate circuit") +
+                                          "; NumPy complex64 restatement of AdaptiveMPS (LAPACK SVD)"}
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -63,6 +63,7 @@ enum agb_desc_field {
   AGB_D_STATUS = 20,  /* (out) per-gate status                                 */
   AGB_D_TOTAL = 21,   /* (out) ||X||_F^2 (double bits)                         */
   AGB_D_NEEDED = 22,  /* (out) eigenpairs actually required (fallback sizing)   */
+  AGB_D_MODE = 23,    /* (out) 1: nothing truncated and m >= n, so A_new = X, B_new = I */
   AGB_D_NFIELDS = 32
 };
 
@@ -133,6 +134,17 @@ int agb_mpo_mix(int dtype, const void* M, const void* W, void* N, int Lw, int Rw
                 void* stream);
 /* out2[0] + i out2[1] = sum_{r,c} E[r,c] Q[c,r]  (double accumulation; out2 is device memory). */
 int agb_trace_prod(int dtype, const void* E, const void* Q, int n, double* out2, void* stream);
+
+/* Per-stage CUDA-event timer of the two-site pipeline (this build's own
+ * instrumentation; no reference counterpart).  agb_prof_begin enables marks on
+ * the launching stream (capacity = max marks); agb_prof_end disables them and
+ * returns summed milliseconds and mark counts per stage id (16 entries):
+ * 0 host gap, 1 setup, 2 contract, 3 gram, 4 tridiag, 5 bisect, 6 invit,
+ * 7 cluster, 8 backtransform, 9 polish, 10 X*V, 11 rank, 12 scatter. */
+int agb_prof_begin(int capacity);
+/* Number of kernels this library has launched since it was loaded. */
+long long agb_launch_count(void);
+int agb_prof_end(double* ms_per_stage, int* marks_per_stage, int nstages);
 
 /* Batched complex GEMM (SIMT reference-free kernel, used by the host layer):
  * C[b] = alpha * op(A[b]) op(B[b]) + beta * C[b]; op: 'N','T','C'. */
