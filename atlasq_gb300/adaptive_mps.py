@@ -289,7 +289,8 @@ class AdaptiveMPS:
             k = int(row[_lib.D_K])
             r = {"status": st, "k": k, "eps_local": _bitsd(int(row[_lib.D_EPSLOC])),
                  "entropy": _bitsd(int(row[_lib.D_ENTROPY])), "condS": _bitsd(int(row[_lib.D_CONDS])),
-                 "chiL": chiL, "chiM": chiM, "chiR": chiR, "driver": "gb300_gram_heevd", "dtype": dt}
+                 "chiL": chiL, "chiM": chiM, "chiR": chiR, "driver": "gb300_gram_heevd", "dtype": dt,
+                 "mode": int(row[_lib.D_MODE]), "ell": int(row[_lib.D_ELL])}
             if st not in (_lib.AGB_OK, _lib.AGB_ERR_RANK):
                 check(st, f"two-site update on bond {i}")
             ok = self._budget_ok_fn(chiL, chiM, chiR, dt)

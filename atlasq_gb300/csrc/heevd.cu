@@ -254,6 +254,9 @@ __global__ void __launch_bounds__(256) bisect_kernel(const HeevdProb* __restrict
 }
 
 // ------------------------------------------------------------------ stage 3
+template <typename R> AGB_DEV R cluster_tol(const R* lam, int ell, double tolrel);
+template <typename R> AGB_DEV bool in_cluster(const R* lam, int ell, int t, R tol);
+
 template <typename R>
 __global__ void __launch_bounds__(128) invit_kernel(const HeevdProb* __restrict__ probs) {
   const HeevdProb P = probs[blockIdx.y];
@@ -269,6 +272,7 @@ __global__ void __launch_bounds__(128) invit_kernel(const HeevdProb* __restrict_
   __syncthreads();
   const int t = blockIdx.x * 128 + threadIdx.x;
   if (t >= ell || P.skip_vectors) return;
+  if (in_cluster((const R*)P.lam, ell, t, cluster_tol((const R*)P.lam, ell, 1e-5))) return;
   const R lam = ((const R*)P.lam)[t];
   R tnorm = 0;
   for (int i = 0; i < n; ++i) tnorm = fmax(tnorm, fabs(d[i]) + fabs(e[i]) + (i ? fabs(e[i - 1]) : R(0)));
@@ -356,53 +360,206 @@ __global__ void __launch_bounds__(128) invit_kernel(const HeevdProb* __restrict_
 }
 
 // ------------------------------------------------------------------ stage 4
+// Eigenvalue clusters (consecutive eigenvalues closer than tolrel * max|lambda|)
+// are solved member by member, as LAPACK's stein does: each member's iterate
+// is re-orthogonalised (classical Gram-Schmidt, twice) against the members
+// already computed before every inverse-iteration solve, and members' shifts
+// are separated by a few ulps.  This keeps the iterates from collapsing onto
+// one direction when T splits (exactly degenerate eigenvalues) or when the
+// cluster sits at the noise floor of the Gram matrix.  One CTA per cluster.
 template <typename R>
-__global__ void __launch_bounds__(256) cluster_mgs_kernel(const HeevdProb* __restrict__ probs, double tolrel) {
-  const HeevdProb P = probs[blockIdx.x];
+AGB_DEV R cluster_tol(const R* lam, int ell, double tolrel) {
+  const R scale = fmax(fabs(lam[0]), fabs(lam[ell - 1]));
+  return (R)tolrel * fmax(scale, rlim<R>::pivmin());
+}
+
+template <typename R>
+AGB_DEV bool in_cluster(const R* lam, int ell, int t, R tol) {
+  const bool left = (t > 0) && (lam[t - 1] - lam[t]) <= tol;
+  const bool right = (t + 1 < ell) && (lam[t] - lam[t + 1]) <= tol;
+  return left || right;
+}
+
+// LU with partial pivoting of T - lam I into the interleaved factor arrays
+// (column t of each), as in invit_kernel.
+template <typename R>
+AGB_DEV void tri_lu(const R* d, const R* e, int n, R lam, R piv, R* U0, R* U1, R* U2, R* Lm, R* Pv,
+                    int64_t L, int t) {
+  R u0 = d[0] - lam, u1 = (n > 1) ? e[0] : R(0), u2 = 0;
+  for (int i = 0; i < n - 1; ++i) {
+    const R sub = e[i], nd = d[i + 1] - lam, ns = (i + 1 < n - 1) ? e[i + 1] : R(0);
+    R a0, a1, a2, m, pv;
+    if (fabs(u0) >= fabs(sub)) {
+      if (u0 == R(0)) u0 = piv;
+      m = sub / u0;
+      a0 = u0; a1 = u1; a2 = u2;
+      u0 = nd - m * u1;
+      u1 = ns - m * u2;
+      pv = 0;
+    } else {
+      m = u0 / sub;
+      a0 = sub; a1 = nd; a2 = ns;
+      const R nu0 = u1 - m * nd, nu1 = u2 - m * ns;
+      u0 = nu0;
+      u1 = nu1;
+      pv = 1;
+    }
+    u2 = 0;
+    U0[i * L + t] = a0;
+    U1[i * L + t] = a1;
+    U2[i * L + t] = a2;
+    Lm[i * L + t] = m;
+    Pv[i * L + t] = pv;
+  }
+  if (fabs(u0) < piv) u0 = copysign(piv, u0 == R(0) ? R(1) : u0);
+  U0[(int64_t)(n - 1) * L + t] = u0;
+  U1[(int64_t)(n - 1) * L + t] = 0;
+  U2[(int64_t)(n - 1) * L + t] = 0;
+}
+
+// In place: y <- (T - lam I)^{-1} y using the stored factors; returns ||y||^2.
+template <typename R>
+AGB_DEV R tri_solve(R* Y, int n, const R* U0, const R* U1, const R* U2, const R* Lm, const R* Pv,
+                    int64_t L, int t, R piv) {
+  R bi = Y[t];
+  for (int i = 0; i < n - 1; ++i) {
+    R bn = Y[(i + 1) * L + t];
+    if (Pv[i * L + t] != R(0)) {
+      const R tmp = bi;
+      bi = bn;
+      bn = tmp;
+    }
+    Y[i * L + t] = bi;
+    bi = bn - Lm[i * L + t] * bi;
+  }
+  Y[(int64_t)(n - 1) * L + t] = bi;
+  R x1 = 0, x2 = 0, nrm = 0;
+  for (int i = n - 1; i >= 0; --i) {
+    R u = U0[i * L + t];
+    if (fabs(u) < piv) u = copysign(piv, u == R(0) ? R(1) : u);
+    const R x = (Y[i * L + t] - U1[i * L + t] * x1 - U2[i * L + t] * x2) / u;
+    Y[i * L + t] = x;
+    nrm += x * x;
+    x2 = x1;
+    x1 = x;
+  }
+  return nrm;
+}
+
+// CGS2 of column j against columns [t0, j) and normalisation (block-wide).
+template <typename R>
+AGB_DEV void cgs2_normalize(R* Y, int n, int64_t L, int t0, int j, R* coef, R* red) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int pass = 0; pass < 2; ++pass) {
+    if (j > t0) {
+      for (int i = t0 + tid; i < j; i += nt) {
+        R acc = 0;
+        for (int r = 0; r < n; ++r) acc += Y[r * L + i] * Y[r * L + j];
+        coef[i - t0] = acc;
+      }
+      __syncthreads();
+      for (int r = tid; r < n; r += nt) {
+        R acc = 0;
+        for (int i = t0; i < j; ++i) acc += coef[i - t0] * Y[r * L + i];
+        Y[r * L + j] -= acc;
+      }
+      __syncthreads();
+    }
+  }
+  R part = 0;
+  for (int r = tid; r < n; r += nt) part += Y[r * L + j] * Y[r * L + j];
+  const R nrm = block_sum(part, red);
+  const R sc = R(1) / sqrt(fmax(nrm, rlim<R>::pivmin()));
+  for (int r = tid; r < n; r += nt) Y[r * L + j] *= sc;
+  __syncthreads();
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) cluster_invit_kernel(const HeevdProb* __restrict__ probs, double tolrel) {
+  const HeevdProb P = probs[blockIdx.y];
   const int n = P.n, ell = P.ell;
   if (ell < 2 || P.skip_vectors) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  int* start = (int*)smem_raw;  // cluster start for each index
-  const R* lam = (const R*)P.lam;
-  if (threadIdx.x == 0) {
-    const R scale = fmax(fabs(lam[0]), fabs(lam[ell - 1]));
-    const R tol = (R)tolrel * fmax(scale, rlim<R>::pivmin());
-    int s = 0;
-    for (int t = 0; t < ell; ++t) {
-      if (t > 0 && (lam[t - 1] - lam[t]) > tol) s = t;
-      start[t] = s;
-    }
-  }
+  R* d = (R*)smem_raw;   // [n]
+  R* e = d + n;          // [n]
+  R* coef = e + n;       // [ell]
+  R* f = coef + ell;     // [5n] LU factors of the current member (U0,U1,U2,L,P)
+  R* ycol = f + 5 * n;   // [n]  working column for the serial solve
+  __shared__ int cl_t0, cl_t1;
+  __shared__ R red[32];
+  __shared__ R s_shift, s_nrm;
+  const R* lamg = (const R*)P.lam;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int t = tid; t < ell; t += nt) coef[t] = lamg[t];  // scan the eigenvalues from shared memory
   __syncthreads();
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  R* Y = (R*)P.Y;
-  const int64_t L = ell;
-  // a warp owns a cluster if it owns the cluster's first index (round robin by start)
-  int cid = 0;
-  for (int t = 0; t < ell; ++t) {
-    if (start[t] != t) continue;
-    int end = t + 1;
-    while (end < ell && start[end] == t) ++end;
-    const bool mine = (cid % nw) == wid;
-    ++cid;
-    if (!mine || end - t < 2) continue;
-    for (int pass = 0; pass < 2; ++pass) {
-      for (int j = t; j < end; ++j) {
-        for (int i = t; i < j; ++i) {
-          R dot = 0;
-          for (int r = lane; r < n; r += 32) dot += Y[r * L + i] * Y[r * L + j];
-          dot = warp_sum(dot);
-          for (int r = lane; r < n; r += 32) Y[r * L + j] -= dot * Y[r * L + i];
-          __syncwarp();
+  const R* lam = coef;
+  if (tid == 0) {
+    const R tol = cluster_tol(lam, ell, tolrel);
+    int found = -1, s = 0, t0 = -1, t1 = -1;
+    for (int t = 1; t <= ell; ++t) {
+      if (t == ell || (lam[t - 1] - lam[t]) > tol) {
+        if (t - s > 1) {
+          ++found;
+          if (found == (int)blockIdx.x) {
+            t0 = s;
+            t1 = t;
+            break;
+          }
         }
-        R nrm = 0;
-        for (int r = lane; r < n; r += 32) nrm += Y[r * L + j] * Y[r * L + j];
-        nrm = warp_sum(nrm);
-        const R s = R(1) / sqrt(fmax(nrm, rlim<R>::pivmin()));
-        for (int r = lane; r < n; r += 32) Y[r * L + j] *= s;
-        __syncwarp();
+        s = t;
       }
     }
+    cl_t0 = t0;
+    cl_t1 = t1;
+  }
+  __syncthreads();
+  const int t0 = cl_t0, t1 = cl_t1;
+  if (t0 < 0) return;
+  __syncthreads();  // the eigenvalue copy in coef is dead from here on
+  for (int i = tid; i < n; i += nt) {
+    d[i] = ((const R*)P.d)[i];
+    e[i] = (i < n - 1) ? ((const R*)P.e)[i] : R(0);
+  }
+  __syncthreads();
+  R tnorm = 0;
+  for (int i = 0; i < n; ++i) tnorm = fmax(tnorm, fabs(d[i]) + fabs(e[i]) + (i ? fabs(e[i - 1]) : R(0)));
+  const R piv = rlim<R>::eps() * fmax(tnorm, rlim<R>::pivmin());
+  const R pert = R(10) * rlim<R>::eps() * fmax(tnorm, rlim<R>::pivmin());
+  R* lu = (R*)P.lu;
+  const int64_t L = ell;
+  R* U0 = lu;
+  R* U1 = lu + (int64_t)n * L;
+  R* U2 = lu + 2 * (int64_t)n * L;
+  R* Lm = lu + 3 * (int64_t)n * L;
+  R* Pv = lu + 4 * (int64_t)n * L;
+  R* Y = (R*)P.Y;
+  (void)U0; (void)U1; (void)U2; (void)Lm; (void)Pv;
+  R prev = 0;
+  for (int j = t0; j < t1; ++j) {
+    if (tid == 0) {
+      R sh = lamg[j];
+      if (j > t0 && sh > prev - pert) sh = prev - pert;  // separate the shifts (descending)
+      s_shift = sh;
+      tri_lu(d, e, n, sh, piv, f, f + n, f + 2 * n, f + 3 * n, f + 4 * n, 1, 0);
+    }
+    for (int r = tid; r < n; r += nt) Y[r * L + j] = (R)philox_normal(P.seed, (uint64_t)j * (uint64_t)n + r, 0x11u);
+    __syncthreads();
+    prev = s_shift;
+    for (int it = 0; it < 2; ++it) {
+      cgs2_normalize(Y, n, L, t0, j, coef, red);
+      for (int r = tid; r < n; r += nt) ycol[r] = Y[r * L + j];
+      __syncthreads();
+      if (tid == 0) s_nrm = tri_solve(ycol, n, f, f + n, f + 2 * n, f + 3 * n, f + 4 * n, 1, 0, piv);
+      __syncthreads();
+      for (int r = tid; r < n; r += nt) Y[r * L + j] = ycol[r];
+      __syncthreads();
+      if (!(s_nrm < R(1e300)) || !(s_nrm > R(0))) {
+        for (int r = tid; r < n; r += nt)
+          Y[r * L + j] = (R)philox_normal(P.seed ^ 0xABCDEFull, (uint64_t)(j + it + 1) * (uint64_t)n + r, 0x13u);
+        __syncthreads();
+      }
+    }
+    cgs2_normalize(Y, n, L, t0, j, coef, red);
   }
 }
 
@@ -550,8 +707,14 @@ int launch_heevd_vectors(HeevdProb* probs, GemmProb* gp, int count, int maxn, in
   invit_kernel<R><<<dim3((maxell + 127) / 128, count), 128, sm_r, s>>>(probs);
   AGB_CHECK_LAUNCH();
   prof_mark(AGB_ST_CLUSTER, s);
-  cluster_mgs_kernel<R><<<count, 256, (size_t)maxell * sizeof(int), s>>>(probs, 1e-5);
-  AGB_CHECK_LAUNCH();
+  {
+    const size_t sm = (8 * (size_t)maxn + (size_t)maxell) * sizeof(R);
+    if (sm > 48 * 1024)
+      cudaFuncSetAttribute(cluster_invit_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    const int maxcl = maxell / 2 > 0 ? maxell / 2 : 1;
+    cluster_invit_kernel<R><<<dim3(maxcl, count), 256, sm, s>>>(probs, 1e-5);
+    AGB_CHECK_LAUNCH();
+  }
   int rc;
   prof_mark(AGB_ST_BACKTRANS, s);
   if (maxn <= 128) rc = launch_bt<CX, 4>(probs, count, maxell, s);
