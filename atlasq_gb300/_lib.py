@@ -19,6 +19,7 @@ AGB_ERR_TIMEOUT = 4
 AGB_ERR_CUDA = 5
 AGB_ERR_UNSUPPORTED = 6
 AGB_ERR_RANK = 7
+AGB_ERR_TOO_LARGE = 8
 
 AGB_C64 = 0
 AGB_C128 = 1
@@ -40,6 +41,7 @@ _ERRS = {
     AGB_ERR_CUDA: (RuntimeError, "CUDA launch failed"),
     AGB_ERR_UNSUPPORTED: (NotImplementedError, "size or mode not supported"),
     AGB_ERR_RANK: (RuntimeError, "eigenpairs computed below the required rank"),
+    AGB_ERR_TOO_LARGE: (ValueError, "problem exceeds the fixed scratch of the allocation-free entry point"),
 }
 
 _lib = None
@@ -62,6 +64,7 @@ _SIGS = {
     "agb_heevd": (I, [I, I, I, I, P, P, P, P, SZ, U64, P]),
     "agb_qr_workspace": (SZ, [I, I, I]),
     "agb_qr": (I, [I, P, I, I, I, P, P, I, P, SZ, P]),
+    "agb_qr_noalloc": (I, [I, P, I, I, I, P, P, I, P]),
     "agb_sample_site": (I, [I, P, I, I, I, U64, U64, P, P, P, P]),
     "agb_mpo_mix": (I, [I, P, P, P, I, I, I, I, P]),
     "agb_trace_prod": (I, [I, P, P, I, P, P]),

@@ -162,3 +162,74 @@ extern "C" int agb_qr(int dtype, const void* A, int M, int N, int transA, void* 
   AGB_CHECK_LAUNCH();
   return AGB_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Allocation-free QR.
+//
+// Some callers of this library cannot allocate device memory: a host runtime
+// that reaches the library only through this C ABI and is handed device
+// pointers by the component that owns the GPU memory, or code running while
+// another allocator owns every device allocation.  agb_qr_noalloc computes the
+// same factorisation as agb_qr without a caller-supplied workspace: its scratch
+// (the working copy of op(A) and the reflector scalars) is the file-scope
+// device array below, AGB_QR_NOALLOC_MAX_BYTES bytes, which every GPU that
+// loads this library holds until the process exits.
+//
+// * The array's host-side name is not a device address.  The first call on
+//   each device, with that device current, looks the address up with
+//   cudaGetSymbolAddress and caches it; make that first call before any
+//   stream capture begins.
+// * Every call shares the one array and it keeps the previous call's
+//   contents.  The kernel overwrites everything it reads (the working copy is
+//   filled from A, each scalar is written before use), so nothing has to be
+//   cleared first.  Calls that overlap on the GPU (e.g. on two streams) race
+//   on the array; issue them on one stream or serialise them.
+// * Problems whose scratch exceeds AGB_QR_NOALLOC_MAX_BYTES are rejected with
+//   AGB_ERR_TOO_LARGE before anything is launched.
+// * No cudaMalloc, cudaFree or allocating library call is made.
+#include <mutex>
+
+static __device__ __align__(256) unsigned char g_qr_noalloc_scratch[AGB_QR_NOALLOC_MAX_BYTES];
+
+namespace {
+constexpr int kMaxDevices = 64;
+void* g_qr_noalloc_ptr[kMaxDevices] = {nullptr};
+std::mutex g_qr_noalloc_mu;
+}  // namespace
+
+extern "C" int agb_qr_noalloc(int dtype, const void* A, int M, int N, int transA, void* Q, void* R,
+                              int trans_out, void* stream) {
+  if (dtype != AGB_C64 && dtype != AGB_C128) return AGB_ERR_ARG;
+  if (M <= 0 || N <= 0 || !A || !Q || !R) return AGB_ERR_ARG;
+  if (M > 8192) return AGB_ERR_UNSUPPORTED;
+  const size_t need = agb_qr_workspace(dtype, M, N);
+  if (need > (size_t)AGB_QR_NOALLOC_MAX_BYTES) return AGB_ERR_TOO_LARGE;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return AGB_ERR_CUDA;
+  void* base = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_qr_noalloc_mu);
+    if (!g_qr_noalloc_ptr[dev]) {
+      void* p = nullptr;
+      if (cudaGetSymbolAddress(&p, g_qr_noalloc_scratch) != cudaSuccess || !p) return AGB_ERR_CUDA;
+      g_qr_noalloc_ptr[dev] = p;
+    }
+    base = g_qr_noalloc_ptr[dev];
+  }
+  const int esz = dtype == AGB_C64 ? 8 : 16;
+  void* W = base;
+  void* tau = (char*)base + agb_align((size_t)M * N * esz);
+  const size_t smem = (size_t)M * esz + (size_t)QR_RG * QR_CG * esz;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (dtype == AGB_C64) {
+    if (smem > 48 * 1024) cudaFuncSetAttribute(qr_kernel<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    qr_kernel<float2><<<1, 1024, smem, s>>>((const float2*)A, M, N, transA, (float2*)W, (float2*)Q,
+                                             (float2*)R, trans_out, (float2*)tau);
+  } else {
+    if (smem > 48 * 1024) cudaFuncSetAttribute(qr_kernel<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    qr_kernel<double2><<<1, 1024, smem, s>>>((const double2*)A, M, N, transA, (double2*)W,
+                                              (double2*)Q, (double2*)R, trans_out, (double2*)tau);
+  }
+  AGB_CHECK_LAUNCH();
+  return AGB_OK;
+}

@@ -31,6 +31,7 @@ extern "C" {
 #define AGB_ERR_CUDA 5         /* CUDA launch / runtime error */
 #define AGB_ERR_UNSUPPORTED 6  /* size or mode not supported by this build */
 #define AGB_ERR_RANK 7         /* eigenpairs computed < rank required (caller re-plans) */
+#define AGB_ERR_TOO_LARGE 8    /* problem exceeds the fixed scratch of agb_qr_noalloc */
 
 /* dtype codes */
 #define AGB_C64 0
@@ -118,6 +119,20 @@ int agb_heevd(int dtype, int batch, int n, int ell, void* H, void* evals, void* 
 size_t agb_qr_workspace(int dtype, int M, int N);
 int agb_qr(int dtype, const void* A, int M, int N, int transA, void* Q, void* R, int trans_out,
            void* ws, size_t ws_bytes, void* stream);
+
+/* Allocation-free variant of agb_qr (no counterpart in the reference).
+ * For callers that cannot allocate device memory -- e.g. a host runtime that
+ * reaches this library only through the C ABI with device pointers handed to
+ * it by the owner of the GPU memory.  Same arguments and results as agb_qr but
+ * no workspace: the scratch is a fixed device array of AGB_QR_NOALLOC_MAX_BYTES
+ * (8 MiB, held by every GPU that loads the library) -- problems needing more
+ * (agb_qr_workspace(dtype, M, N) > the limit) return AGB_ERR_TOO_LARGE.  The
+ * first call on a device looks up the array's address (cudaGetSymbolAddress):
+ * make it before any stream capture.  All calls share the array, so calls that
+ * overlap on the GPU race; serialise them.  Allocates nothing. */
+#define AGB_QR_NOALLOC_MAX_BYTES (8u << 20)
+int agb_qr_noalloc(int dtype, const void* A, int M, int N, int transA, void* Q, void* R, int trans_out,
+                   void* stream);
 
 /* (a9) One site of batched sequential-conditional sampling.
  * Replaces the per-site body of _batch_sweep_sample (src/atlas_q/mps_pytorch.py:282-352)
