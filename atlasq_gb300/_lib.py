@@ -71,6 +71,9 @@ _SIGS = {
     "agb_prof_begin": (I, [I]),
     "agb_launch_count": (ctypes.c_longlong, []),
     "agb_prof_end": (I, [P, P, I]),
+    "agb_cgemm_tc_workspace": (SZ, [I, I, I, I]),
+    "agb_cgemm_tc": (I, [ctypes.c_char, ctypes.c_char, I, I, I, I, P, I64, I64, P, I64, I64, P, I64, I64,
+                         ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, P, SZ, P, P]),
     "agb_cgemm_batched": (I, [I, ctypes.c_char, ctypes.c_char, I, I, I, I, P, I64, I64, P, I64, I64,
                               P, I64, I64, D, D, D, D, P]),
 }

@@ -16,7 +16,18 @@ struct GemmProb {
   double alpha_re, alpha_im, beta_re, beta_im;
 };
 
-// Launch the SIMT tile kernel over `count` problems whose M, N are bounded by
-// maxM, maxN (tiles beyond a problem's own extent exit early).
+// Optional tensor-core context: scratch for the packed split operands and a
+// device status word.  With a context whose scratch is large enough,
+// complex64 problems of at least 64 x 64 x 32 run on tcgen05 (gemm_tc.cu);
+// everything else runs on the SIMT kernel.
+struct GemmCtx {
+  void* tc_scratch = nullptr;
+  size_t tc_bytes = 0;
+  int* status = nullptr;
+};
+
+// Launch over `count` problems whose M, N, K are bounded by maxM, maxN, maxK
+// (tiles beyond a problem's own extent exit early).
 template <typename CX>
-int launch_gemm_probs(const GemmProb* probs, int count, int maxM, int maxN, cudaStream_t s);
+int launch_gemm_probs(const GemmProb* probs, int count, int maxM, int maxN, cudaStream_t s,
+                      const GemmCtx* ctx = nullptr, int maxK = 0);

@@ -2,6 +2,7 @@
 // 256 threads, 4x4 complex accumulators per thread.  Used for small and ragged
 // shapes, and for complex128.
 #include "gemm.cuh"
+#include "gemm_tc.cuh"
 
 namespace {
 
@@ -100,8 +101,12 @@ __global__ void __launch_bounds__(256) gemm_simt_kernel(const GemmProb* __restri
 }  // namespace
 
 template <typename CX>
-int launch_gemm_probs(const GemmProb* probs, int count, int maxM, int maxN, cudaStream_t s) {
+int launch_gemm_probs(const GemmProb* probs, int count, int maxM, int maxN, cudaStream_t s, const GemmCtx* ctx,
+                      int maxK) {
   if (count <= 0 || maxM <= 0 || maxN <= 0) return AGB_OK;
+  if (sizeof(CX) == 8 && ctx && ctx->tc_scratch && maxM >= 64 && maxN >= 64 && maxK >= 32 &&
+      ctx->tc_bytes >= tc_gemm_scratch_bytes(count, maxM, maxN, maxK))
+    return launch_gemm_tc(probs, count, maxM, maxN, maxK, ctx->tc_scratch, ctx->tc_bytes, ctx->status, s);
   dim3 grid((maxN + BN - 1) / BN, (maxM + BM - 1) / BM, count);
   StridedBatch sb = {};
   gemm_simt_kernel<CX><<<grid, 256, 0, s>>>(probs, sb);
@@ -109,8 +114,8 @@ int launch_gemm_probs(const GemmProb* probs, int count, int maxM, int maxN, cuda
   return AGB_OK;
 }
 
-template int launch_gemm_probs<float2>(const GemmProb*, int, int, int, cudaStream_t);
-template int launch_gemm_probs<double2>(const GemmProb*, int, int, int, cudaStream_t);
+template int launch_gemm_probs<float2>(const GemmProb*, int, int, int, cudaStream_t, const GemmCtx*, int);
+template int launch_gemm_probs<double2>(const GemmProb*, int, int, int, cudaStream_t, const GemmCtx*, int);
 
 namespace {
 int op_code(char c) { return (c == 'N' || c == 'n') ? 0 : (c == 'T' || c == 't') ? 1 : (c == 'C' || c == 'c') ? 2 : -1; }

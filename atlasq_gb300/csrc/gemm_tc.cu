@@ -1,0 +1,438 @@
+// Batched complex GEMM on the 5th-generation tensor cores (sm_103a):
+// D = alpha * op(A) op(B) + beta * Csrc, complex64, split precision 3xTF32.
+//
+// 1. pack_kernel writes op(A) (M x K) and op(B)^T (N x K) of every problem into
+//    planar, K-major, zero-padded fp32 planes  [problem][plane][row][k]  with
+//    plane = {Re_hi, Re_lo, Im_hi, Im_lo}: hi = x rounded to TF32 (11-bit
+//    significand), lo = x - hi.  Conjugation is folded into the Im planes.
+// 2. tc_gemm_kernel: one CTA (4 warps) per 128 x 64 output tile.  Warp 0 lane 0
+//    streams 32-wide K slices of the eight planes into shared memory with TMA
+//    (cp.async.bulk.tensor, 128-byte swizzle) through a 2-stage mbarrier
+//    pipeline; warp 1 lane 0 issues tcgen05.mma.kind::tf32 (M=128, N=64, K=8):
+//       Re += Ar_h Br_h + Ar_h Br_l + Ar_l Br_h - (Ai_h Bi_h + Ai_h Bi_l + Ai_l Bi_h)
+//       Im += Ar_h Bi_h + Ar_h Bi_l + Ar_l Bi_h +  Ai_h Br_h + Ai_h Br_l + Ai_l Br_h
+//    into two fp32 accumulators in tensor memory (columns 0-63 and 64-127; the
+//    minus sign is the instruction descriptor's negate-A bit).  All warps then
+//    read the accumulators with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31
+//    = tile rows) and write alpha*C + beta*Csrc.
+// Every mbarrier wait is bounded; on expiry the kernel records AGB_ERR_TIMEOUT
+// in a device status word, drains its copies and frees its tensor memory.
+#include <cuda.h>
+
+#include "gemm.cuh"
+#include "gemm_tc.cuh"
+
+namespace {
+
+constexpr int BM = 128, BN = 64, BK = 32, STAGES = 2;
+constexpr int TILE_A = BM * BK * 4;                    // 16 KiB per plane
+constexpr int TILE_B = BN * BK * 4;                    // 8 KiB per plane
+constexpr int STAGE_BYTES = 4 * TILE_A + 4 * TILE_B;   // 96 KiB
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+constexpr int NACC = 4;                                // k-tiles rotate over 4 accumulator pairs
+constexpr int TMEM_COLS = 2 * BN * NACC;               // 512 columns: (Re, Im) x 4
+constexpr unsigned WAIT_LIMIT = 1u << 26;              // bounded spin (~seconds)
+
+AGB_DEV uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+AGB_DEV void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+AGB_DEV void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+// true when phase `parity` of the barrier completed; false after WAIT_LIMIT polls
+AGB_DEV bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  const uint32_t a = smem_u32(bar);
+  for (unsigned it = 0; it < WAIT_LIMIT; ++it) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+AGB_DEV void tma_load_4d(void* dst, const CUtensorMap* map, int c0, int c1, int c2, int c3, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(
+          smem_u32(dst)),
+      "l"((uint64_t)map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
+      : "memory");
+}
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row atoms of
+// 1024 B (stride byte offset), descriptor version 1.
+AGB_DEV uint64_t sdesc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)1 << 16;             // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;   // stride byte offset
+  d |= (uint64_t)1 << 46;             // version
+  d |= (uint64_t)2 << 61;             // SWIZZLE_128B
+  return d;
+}
+// Instruction descriptor, kind::tf32: D f32, A/B tf32, K-major, M=128, N=64.
+constexpr uint32_t IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+constexpr uint32_t NEG_A = 1u << 13;
+
+AGB_DEV void umma(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\ttcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+          tmem_d),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+AGB_DEV void umma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+AGB_DEV void tmem_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+AGB_DEV float tf32_hi(float x) {
+  uint32_t b = __float_as_uint(x);
+  if ((b & 0x7F800000u) == 0x7F800000u) return x;  // inf / nan unchanged
+  b = (b + 0xFFFu + ((b >> 13) & 1u)) & 0xFFFFE000u;  // round to nearest even at 13 dropped bits
+  return __uint_as_float(b);
+}
+
+// ------------------------------------------------------------------ pack
+// grid: (ceil(Kpad/32), ceil(Rpad/32), count); block (32, 8).  which = 0: A
+// operand rows = op(A) rows (M); which = 1: B operand rows = op(B) columns (N).
+__global__ void pack_kernel(const GemmProb* __restrict__ probs, float* __restrict__ out, int which, int Rpad, int Kpad) {
+  const GemmProb P = probs[blockIdx.z];
+  __shared__ float2 tile[32][33];
+  const int k0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+  const int rows = which == 0 ? P.M : P.N;
+  const int op = which == 0 ? P.opA : P.opB;
+  const float2* src = (const float2*)(which == 0 ? P.A : P.B);
+  const int64_t ld = which == 0 ? P.lda : P.ldb;
+  // element (r, k) of the row-major operand R x K
+  //   A: op(A)[r][k];  B: op(B)[k][r]
+  // stored form: A op N -> A[r][k]; op T/C -> A[k][r]
+  //              B op N -> B[k][r]; op T/C -> B[r][k]
+  const bool rk_contig = (which == 0) ? (op == 0) : (op != 0);  // memory is [r][k] (k fastest)
+  const bool conj = (op == 2);
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  for (int i = ty; i < 32; i += 8) {
+    float2 v = make_float2(0.f, 0.f);
+    if (rk_contig) {
+      const int r = r0 + i, k = k0 + tx;
+      if (r < rows && k < P.K) v = src[(int64_t)r * ld + k];
+      tile[i][tx] = v;
+    } else {
+      const int k = k0 + i, r = r0 + tx;
+      if (r < rows && k < P.K) v = src[(int64_t)k * ld + r];
+      tile[tx][i] = v;
+    }
+  }
+  __syncthreads();
+  const size_t plane = (size_t)Rpad * Kpad;
+  float* base = out + (size_t)blockIdx.z * 4 * plane;
+  for (int i = ty; i < 32; i += 8) {
+    const int r = r0 + i, k = k0 + tx;
+    if (r >= Rpad || k >= Kpad) continue;
+    float2 v = tile[i][tx];
+    if (conj) v.y = -v.y;
+    const float rh = tf32_hi(v.x), ih = tf32_hi(v.y);
+    const size_t o = (size_t)r * Kpad + k;
+    base[o] = rh;
+    base[plane + o] = v.x - rh;
+    base[2 * plane + o] = ih;
+    base[3 * plane + o] = v.y - ih;
+  }
+}
+
+// ------------------------------------------------------------------ GEMM
+__global__ void __launch_bounds__(128, 1)
+    tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                   const GemmProb* __restrict__ probs, int* __restrict__ status) {
+  const GemmProb P = probs[blockIdx.z];
+  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  if (m0 >= P.M || n0 >= P.N) return;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* full = (uint64_t*)(smem + STAGES * STAGE_BYTES);
+  uint64_t* empty = full + STAGES;
+  uint64_t* done = empty + STAGES;
+  uint32_t* tmem_slot = (uint32_t*)(done + 1);
+  volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nk = (P.K + BK - 1) / BK;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(done, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+  const int b = blockIdx.z;
+  if (warp == 0 && lane == 0) {
+    // ---------------- TMA producer
+    int issued = 0;
+    for (int kt = 0; kt < nk; ++kt) {
+      const int s = kt % STAGES;
+      if (kt >= STAGES && !mbar_wait(&empty[s], ((kt / STAGES) - 1) & 1)) {
+        *abort_flag = 1;
+        break;
+      }
+      if (*abort_flag) break;
+      unsigned char* st = smem + s * STAGE_BYTES;
+      mbar_expect_tx(&full[s], STAGE_BYTES);
+      for (int pl = 0; pl < 4; ++pl) tma_load_4d(st + pl * TILE_A, &tmA, kt * BK, m0, pl, b, &full[s]);
+      for (int pl = 0; pl < 4; ++pl) tma_load_4d(st + 4 * TILE_A + pl * TILE_B, &tmB, kt * BK, n0, pl, b, &full[s]);
+      issued = kt + 1;
+    }
+    if (*abort_flag) {
+      // drain: wait (bounded) until every issued copy has landed before the CTA can exit
+      for (int kt = (issued > STAGES ? issued - STAGES : 0); kt < issued; ++kt)
+        mbar_wait(&full[kt % STAGES], (kt / STAGES) & 1);
+    }
+  } else if (warp == 1 && lane == 0) {
+    // ---------------- MMA issuer
+    // k-tile kt accumulates into pair kt % NACC: four chains of length K/4 instead
+    // of one of length K (the tensor core's fp32 accumulation error grows with
+    // the chain length); the epilogue sums the pairs in fp32.
+    for (int kt = 0; kt < nk; ++kt) {
+      const int s = kt % STAGES;
+      const uint32_t d_re = tmem + (uint32_t)(2 * BN * (kt % NACC)), d_im = d_re + BN;
+      if (!mbar_wait(&full[s], (kt / STAGES) & 1)) {
+        *abort_flag = 1;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t sa = smem_u32(smem + s * STAGE_BYTES);
+      const uint32_t sb = sa + 4 * TILE_A;
+#pragma unroll
+      for (int ks = 0; ks < BK / 8; ++ks) {
+        uint64_t a[4], bb[4];
+#pragma unroll
+        for (int pl = 0; pl < 4; ++pl) {
+          a[pl] = sdesc(sa + pl * TILE_A) + (uint64_t)(ks * 2);   // +32 bytes per K=8 step
+          bb[pl] = sdesc(sb + pl * TILE_B) + (uint64_t)(ks * 2);
+        }
+        const uint32_t first = (kt < NACC && ks == 0) ? 0u : 1u;
+        // real part
+        umma(d_re, a[0], bb[0], IDESC, first);
+        umma(d_re, a[0], bb[1], IDESC, 1);
+        umma(d_re, a[1], bb[0], IDESC, 1);
+        umma(d_re, a[2], bb[2], IDESC | NEG_A, 1);
+        umma(d_re, a[2], bb[3], IDESC | NEG_A, 1);
+        umma(d_re, a[3], bb[2], IDESC | NEG_A, 1);
+        // imaginary part
+        umma(d_im, a[0], bb[2], IDESC, first);
+        umma(d_im, a[0], bb[3], IDESC, 1);
+        umma(d_im, a[1], bb[2], IDESC, 1);
+        umma(d_im, a[2], bb[0], IDESC, 1);
+        umma(d_im, a[2], bb[1], IDESC, 1);
+        umma(d_im, a[3], bb[0], IDESC, 1);
+      }
+      umma_commit(&empty[s]);  // stage s may be refilled once these MMAs retire
+    }
+    umma_commit(done);  // accumulators complete
+  }
+  __syncwarp();
+  // ---------------- epilogue (all 4 warps)
+  const bool ok = mbar_wait(done, 0);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (ok && !*abort_flag) {
+    const int row = m0 + warp * 32 + lane;
+    const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+    float2* D = (float2*)P.D;
+    const float2* C = (const float2*)P.Csrc;
+    const float ar = (float)P.alpha_re, ai = (float)P.alpha_im, br = (float)P.beta_re, bi = (float)P.beta_im;
+    const bool use_beta = (br != 0.f || bi != 0.f);
+    const int nacc = nk < NACC ? nk : NACC;
+#pragma unroll 1
+    for (int c0 = 0; c0 < BN; c0 += 16) {
+      float re[16], im[16];
+      tmem_ld16(tmem + lane_base + c0, re);
+      tmem_ld16(tmem + lane_base + BN + c0, im);
+      if (nk == 0) {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) re[i] = im[i] = 0.f;  // empty inner dimension: product is zero
+      }
+      for (int a = 1; a < nacc; ++a) {
+        float r2[16], i2[16];
+        tmem_ld16(tmem + lane_base + (uint32_t)(2 * BN * a) + c0, r2);
+        tmem_ld16(tmem + lane_base + (uint32_t)(2 * BN * a) + BN + c0, i2);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          re[i] += r2[i];
+          im[i] += i2[i];
+        }
+      }
+      if (row < P.M) {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          const int col = n0 + c0 + i;
+          if (col < P.N) {
+            float2 v = make_float2(ar * re[i] - ai * im[i], ar * im[i] + ai * re[i]);
+            if (use_beta) {
+              const float2 c = C[(int64_t)row * P.ldc + col];
+              v.x += br * c.x - bi * c.y;
+              v.y += br * c.y + bi * c.x;
+            }
+            D[(int64_t)row * P.ldd + col] = v;
+          }
+        }
+      }
+    }
+  } else if (threadIdx.x == 0) {
+    atomicExch(status, AGB_ERR_TIMEOUT);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+  }
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      return nullptr;
+    fn = (EncodeTiledFn)p;
+  }
+  return fn;
+}
+
+bool make_map(CUtensorMap* map, float* base, int rows_pad, int kpad, int count, int box_rows) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) return false;
+  const cuuint64_t dims[4] = {(cuuint64_t)kpad, (cuuint64_t)rows_pad, 4, (cuuint64_t)count};
+  const cuuint64_t strides[3] = {(cuuint64_t)kpad * 4, (cuuint64_t)rows_pad * kpad * 4,
+                                 (cuuint64_t)4 * rows_pad * kpad * 4};
+  const cuuint32_t box[4] = {BK, (cuuint32_t)box_rows, 1, 1};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  return fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+int round_up(int x, int m) { return (x + m - 1) / m * m; }
+
+}  // namespace
+
+size_t tc_gemm_scratch_bytes(int count, int maxM, int maxN, int maxK) {
+  const size_t Mp = round_up(maxM, BM), Np = round_up(maxN, BN), Kp = round_up(maxK, BK);
+  return agb_align((size_t)count * 4 * Mp * Kp * 4) + agb_align((size_t)count * 4 * Np * Kp * 4) + 256;
+}
+
+int launch_gemm_tc(const GemmProb* probs, int count, int maxM, int maxN, int maxK, void* scratch,
+                   size_t scratch_bytes, int* status, cudaStream_t s) {
+  if (count <= 0 || maxM <= 0 || maxN <= 0) return AGB_OK;
+  if (maxK <= 0) return AGB_ERR_ARG;
+  if (count > 65535) return AGB_ERR_UNSUPPORTED;
+  if (scratch_bytes < tc_gemm_scratch_bytes(count, maxM, maxN, maxK)) return AGB_ERR_WORKSPACE;
+  const int Mp = round_up(maxM, BM), Np = round_up(maxN, BN), Kp = round_up(maxK, BK);
+  float* pa = (float*)scratch;
+  float* pb = (float*)((char*)scratch + agb_align((size_t)count * 4 * Mp * Kp * 4));
+  pack_kernel<<<dim3(Kp / 32, Mp / 32, count), dim3(32, 8), 0, s>>>(probs, pa, 0, Mp, Kp);
+  AGB_CHECK_LAUNCH();
+  pack_kernel<<<dim3(Kp / 32, Np / 32, count), dim3(32, 8), 0, s>>>(probs, pb, 1, Np, Kp);
+  AGB_CHECK_LAUNCH();
+  CUtensorMap ma, mb;
+  if (!make_map(&ma, pa, Mp, Kp, count, BM) || !make_map(&mb, pb, Np, Kp, count, BN)) return AGB_ERR_CUDA;
+  static bool attr = false;
+  if (!attr) {
+    if (cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES) != cudaSuccess)
+      return AGB_ERR_CUDA;
+    attr = true;
+  }
+  tc_gemm_kernel<<<dim3(Np / BN, Mp / BM, count), 128, SMEM_BYTES, s>>>(ma, mb, probs, status);
+  AGB_CHECK_LAUNCH();
+  return AGB_OK;
+}
+
+// Strided-batch host entry for the tensor-core GEMM (complex64).
+namespace {
+__global__ void strided_probs_kernel(GemmProb* out, GemmProb base, int count, int64_t sA, int64_t sB, int64_t sC) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  GemmProb p = base;
+  p.A = (const float2*)base.A + (int64_t)i * sA;
+  p.B = (const float2*)base.B + (int64_t)i * sB;
+  p.D = (float2*)base.D + (int64_t)i * sC;
+  p.Csrc = (const float2*)base.Csrc + (int64_t)i * sC;
+  out[i] = p;
+}
+int opc(char c) { return (c == 'N' || c == 'n') ? 0 : (c == 'T' || c == 't') ? 1 : (c == 'C' || c == 'c') ? 2 : -1; }
+}  // namespace
+
+extern "C" size_t agb_cgemm_tc_workspace(int batch, int M, int N, int K) {
+  return agb_align((size_t)batch * sizeof(GemmProb)) + agb_align(sizeof(int)) + tc_gemm_scratch_bytes(batch, M, N, K);
+}
+
+extern "C" int agb_cgemm_tc(char opA, char opB, int batch, int M, int N, int K, const void* A, int64_t lda,
+                            int64_t strideA, const void* B, int64_t ldb, int64_t strideB, void* C, int64_t ldc,
+                            int64_t strideC, float alpha_re, float alpha_im, float beta_re, float beta_im, void* ws,
+                            size_t ws_bytes, int* status_host, void* stream) {
+  const int oa = opc(opA), ob = opc(opB);
+  if (oa < 0 || ob < 0 || batch < 0 || M < 0 || N < 0 || K <= 0 || !ws) return AGB_ERR_ARG;
+  if (batch == 0 || M == 0 || N == 0) return AGB_OK;
+  if (ws_bytes < agb_cgemm_tc_workspace(batch, M, N, K)) return AGB_ERR_WORKSPACE;
+  GemmProb base;
+  base.A = A;
+  base.B = B;
+  base.D = C;
+  base.Csrc = C;
+  base.lda = lda;
+  base.ldb = ldb;
+  base.ldd = ldc;
+  base.ldc = ldc;
+  base.M = M;
+  base.N = N;
+  base.K = K;
+  base.opA = oa;
+  base.opB = ob;
+  base.alpha_re = alpha_re;
+  base.alpha_im = alpha_im;
+  base.beta_re = beta_re;
+  base.beta_im = beta_im;
+  char* w = (char*)ws;
+  GemmProb* probs = (GemmProb*)w;
+  int* status = (int*)(w + agb_align((size_t)batch * sizeof(GemmProb)));
+  void* scratch = w + agb_align((size_t)batch * sizeof(GemmProb)) + agb_align(sizeof(int));
+  cudaStream_t s = (cudaStream_t)stream;
+  if (cudaMemsetAsync(status, 0, sizeof(int), s) != cudaSuccess) return AGB_ERR_CUDA;
+  strided_probs_kernel<<<(batch + 127) / 128, 128, 0, s>>>(probs, base, batch, strideA, strideB, strideC);
+  AGB_CHECK_LAUNCH();
+  int rc = launch_gemm_tc(probs, batch, M, N, K, scratch, ws_bytes - (size_t)((char*)scratch - w), status, s);
+  if (rc) return rc;
+  if (status_host) {
+    if (cudaMemcpyAsync(status_host, status, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess) return AGB_ERR_CUDA;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return AGB_ERR_CUDA;
+    if (*status_host) return *status_host;
+  }
+  return AGB_OK;
+}

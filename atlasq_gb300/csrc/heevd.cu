@@ -699,7 +699,8 @@ int launch_heevd_values(HeevdProb* probs, int count, int maxn, int maxell, cudaS
 }
 
 template <typename CX>
-int launch_heevd_vectors(HeevdProb* probs, GemmProb* gp, int count, int maxn, int maxell, cudaStream_t s) {
+int launch_heevd_vectors(HeevdProb* probs, GemmProb* gp, int count, int maxn, int maxell, cudaStream_t s,
+                         const GemmCtx* ctx) {
   typedef typename cx_traits<CX>::R R;
   if (count <= 0 || maxn <= 0 || maxell <= 0) return AGB_OK;
   const size_t sm_r = 2 * (size_t)maxn * sizeof(R);
@@ -726,8 +727,8 @@ int launch_heevd_vectors(HeevdProb* probs, GemmProb* gp, int count, int maxn, in
   for (int step = 0; step < 4; ++step) {
     polish_setup_kernel<<<(count + 127) / 128, 128, 0, s>>>(probs, gp, count, step & 1);
     AGB_CHECK_LAUNCH();
-    if ((rc = launch_gemm_probs<CX>(gp, count, maxell, maxell, s))) return rc;
-    if ((rc = launch_gemm_probs<CX>(gp + count, count, maxn, maxell, s))) return rc;
+    if ((rc = launch_gemm_probs<CX>(gp, count, maxell, maxell, s, ctx, maxn))) return rc;
+    if ((rc = launch_gemm_probs<CX>(gp + count, count, maxn, maxell, s, ctx, maxell))) return rc;
   }
   return AGB_OK;
 }
@@ -743,8 +744,8 @@ template int launch_heevd<float2>(HeevdProb*, GemmProb*, int, int, int, cudaStre
 template int launch_heevd<double2>(HeevdProb*, GemmProb*, int, int, int, cudaStream_t);
 template int launch_heevd_values<float2>(HeevdProb*, int, int, int, cudaStream_t);
 template int launch_heevd_values<double2>(HeevdProb*, int, int, int, cudaStream_t);
-template int launch_heevd_vectors<float2>(HeevdProb*, GemmProb*, int, int, int, cudaStream_t);
-template int launch_heevd_vectors<double2>(HeevdProb*, GemmProb*, int, int, int, cudaStream_t);
+template int launch_heevd_vectors<float2>(HeevdProb*, GemmProb*, int, int, int, cudaStream_t, const GemmCtx*);
+template int launch_heevd_vectors<double2>(HeevdProb*, GemmProb*, int, int, int, cudaStream_t, const GemmCtx*);
 
 // ------------------------------------------------------------------ standalone entry
 namespace {

@@ -81,4 +81,4 @@ template <typename CX>
 int launch_heevd_values(HeevdProb* probs, int count, int maxn, int maxell, cudaStream_t s);
 template <typename CX>
 int launch_heevd_vectors(HeevdProb* probs, GemmProb* gemm_scratch, int count, int maxn, int maxell,
-                         cudaStream_t s);
+                         cudaStream_t s, const GemmCtx* ctx = nullptr);

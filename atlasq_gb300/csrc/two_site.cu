@@ -12,6 +12,7 @@
 // is the projection of X onto the kept right singular subspace.
 #include <math.h>
 
+#include "gemm_tc.cuh"
 #include "heevd.cuh"
 #include "prof.cuh"
 
@@ -64,7 +65,24 @@ struct ContractProb {
 
 AGB_HD size_t header_bytes(int ng) {
   return agb_align((size_t)ng * sizeof(HeevdProb)) + agb_align((size_t)ng * 4 * sizeof(GemmProb)) +
-         agb_align((size_t)ng * sizeof(ContractProb));
+         agb_align((size_t)ng * sizeof(ContractProb)) + 256;  // + tensor-core status word
+}
+AGB_HD int* status_word(char* ws, int ng) { return (int*)(ws + header_bytes(ng) - 256); }
+
+// Packed-operand scratch for the tensor-core GEMMs of a batch (complex64 only),
+// sized for the largest of Gram (n x n, K = m), X V (m x ell, K = n) and the
+// polish products (ell x ell, K = n; n x ell, K = ell); it occupies the last
+// bytes of the workspace.
+size_t tc_tail_bytes(int dtype, int ng, int maxm, int maxn, int maxell) {
+  if (dtype != AGB_C64 || ng <= 0) return 0;
+  size_t b = tc_gemm_scratch_bytes(ng, maxn, maxn, maxm);
+  size_t t = tc_gemm_scratch_bytes(ng, maxm, maxell, maxn);
+  if (t > b) b = t;
+  t = tc_gemm_scratch_bytes(ng, maxell, maxell, maxn);
+  if (t > b) b = t;
+  t = tc_gemm_scratch_bytes(ng, maxn, maxell, maxell);
+  if (t > b) b = t;
+  return agb_align(b);
 }
 
 // ------------------------------------------------------------------ setup
@@ -401,6 +419,10 @@ __global__ void __launch_bounds__(1024) rank_kernel(int64_t* __restrict__ desc, 
     status = AGB_ERR_NOCONV;
     k = 0;
   }
+  if (*status_word(ws, ng) != 0) {  // a bounded wait in a tensor-core GEMM expired
+    status = *status_word(ws, ng);
+    k = 0;
+  }
   D[AGB_D_K] = k;
   D[AGB_D_EPSLOC] = bitsd(eps_local);
   D[AGB_D_ENTROPY] = bitsd(entropy);
@@ -454,8 +476,10 @@ __global__ void scatter_kernel(const int64_t* __restrict__ desc, char* ws) {
 }
 
 template <typename CX>
-int run_impl(int ng, int64_t* desc, int maxL, int maxM, int maxR, int maxell, char* ws, cudaStream_t s) {
+int run_impl(int ng, int64_t* desc, int maxL, int maxM, int maxR, int maxell, char* ws, size_t ws_bytes,
+             size_t tc_bytes, cudaStream_t s) {
   const int esz = sizeof(CX);
+  if (cudaMemsetAsync(status_word(ws, ng), 0, sizeof(int), s) != cudaSuccess) return AGB_ERR_CUDA;
   prof_mark(AGB_ST_SETUP, s);
   setup_kernel<<<(ng + 127) / 128, 128, 0, s>>>(desc, ng, ws, esz);
   AGB_CHECK_LAUNCH();
@@ -468,17 +492,21 @@ int run_impl(int ng, int64_t* desc, int maxL, int maxM, int maxR, int maxell, ch
   contract_gate_kernel<CX><<<dim3((maxR + 15) / 16, (maxL + 15) / 16, ng), 256, 0, s>>>(cp, none);
   AGB_CHECK_LAUNCH();
   const int maxm = 2 * maxL, maxn = 2 * maxR;
+  GemmCtx ctx;
+  ctx.tc_bytes = tc_bytes;
+  ctx.tc_scratch = tc_bytes ? ws + ws_bytes - tc_bytes : nullptr;
+  ctx.status = status_word(ws, ng);
   prof_mark(AGB_ST_GRAM, s);
-  int rc = launch_gemm_probs<CX>(gp + 2 * ng, ng, maxn, maxn, s);
+  int rc = launch_gemm_probs<CX>(gp + 2 * ng, ng, maxn, maxn, s, &ctx, maxm);
   if (rc) return rc;
   rc = launch_heevd_values<CX>(hp, ng, maxn, maxell, s);
   if (rc) return rc;
   prerank_kernel<CX><<<(ng + 127) / 128, 128, 0, s>>>(desc, ng, ws);
   AGB_CHECK_LAUNCH();
-  rc = launch_heevd_vectors<CX>(hp, gp, ng, maxn, maxell, s);
+  rc = launch_heevd_vectors<CX>(hp, gp, ng, maxn, maxell, s, &ctx);
   if (rc) return rc;
   prof_mark(AGB_ST_AV, s);
-  rc = launch_gemm_probs<CX>(gp + 3 * ng, ng, maxm, maxell, s);
+  rc = launch_gemm_probs<CX>(gp + 3 * ng, ng, maxm, maxell, s, &ctx, maxn);
   if (rc) return rc;
   prof_mark(AGB_ST_RANK, s);
   rank_kernel<CX><<<ng, 1024, 2 * (size_t)maxell * sizeof(double), s>>>(desc, ng, ws);
@@ -531,7 +559,14 @@ extern "C" int agb_two_site_plan(int dtype, int ng, int64_t* desc, size_t* ws_by
     D[AGB_D_WS] = (int64_t)off;
     off += agb_align(slab_layout(m, n, ell, esz).total);
   }
-  *ws_bytes = off;
+  int mL = 1, mR = 1, mE = 1;
+  for (int g = 0; g < ng; ++g) {
+    const int64_t* D = desc + (int64_t)g * AGB_D_NFIELDS;
+    mL = (int)D[AGB_D_CHIL] > mL ? (int)D[AGB_D_CHIL] : mL;
+    mR = (int)D[AGB_D_CHIR] > mR ? (int)D[AGB_D_CHIR] : mR;
+    mE = (int)D[AGB_D_ELL] > mE ? (int)D[AGB_D_ELL] : mE;
+  }
+  *ws_bytes = off + tc_tail_bytes(dtype, ng, 2 * mL, 2 * mR, mE);
   return AGB_OK;
 }
 
@@ -545,10 +580,11 @@ extern "C" int agb_two_site_run(int dtype, int ng, const int64_t* desc_dev, int6
   if (!desc_out || !ws || max_chiL <= 0 || max_chiR <= 0 || max_ell <= 0) return AGB_ERR_ARG;
   if (2 * max_chiR > 1024 || max_ell > 1024) return AGB_ERR_UNSUPPORTED;
   if (ws_bytes < header_bytes(ng)) return AGB_ERR_WORKSPACE;
+  const size_t tc = tc_tail_bytes(dtype, ng, 2 * max_chiL, 2 * max_chiR, max_ell);
   cudaStream_t s = (cudaStream_t)stream;
   if (dtype == AGB_C64)
-    return run_impl<float2>(ng, desc_out, max_chiL, max_chiM, max_chiR, max_ell, (char*)ws, s);
-  return run_impl<double2>(ng, desc_out, max_chiL, max_chiM, max_chiR, max_ell, (char*)ws, s);
+    return run_impl<float2>(ng, desc_out, max_chiL, max_chiM, max_chiR, max_ell, (char*)ws, ws_bytes, tc, s);
+  return run_impl<double2>(ng, desc_out, max_chiL, max_chiM, max_chiR, max_ell, (char*)ws, ws_bytes, tc, s);
 }
 
 extern "C" int agb_two_site_finalize(int dtype, int ng, const int64_t* desc_dev, int max_chiL,

@@ -115,3 +115,33 @@ def single_qubit_gate_(T, U):
     check(lib.agb_single_qubit_gate(dtype_code(T.dtype), ptr(T), ptr(U), T.shape[0], T.shape[2],
                                     stream_ptr(T.device)), "single_qubit_gate")
     return T
+
+
+def cgemm_tc(A, B, opA="N", opB="N", alpha=1.0, beta=0.0, C=None):
+    """complex64 GEMM on the tcgen05 tensor cores (3xTF32); same contract as cgemm."""
+    lib = _lib.load()
+    A, B = _c(A), _c(B)
+    if A.dtype != torch.complex64:
+        raise ValueError("cgemm_tc takes complex64")
+    batched = A.dim() == 3
+    A2, B2 = (A, B) if batched else (A.unsqueeze(0), B.unsqueeze(0))
+    bat = A2.shape[0]
+    ra, ca = A2.shape[1], A2.shape[2]
+    rb, cb = B2.shape[1], B2.shape[2]
+    M, K = (ra, ca) if opA == "N" else (ca, ra)
+    K2, N = (rb, cb) if opB == "N" else (cb, rb)
+    if K != K2:
+        raise ValueError(f"inner dimension mismatch {K} vs {K2}")
+    if C is None:
+        C = torch.empty(bat, M, N, dtype=A.dtype, device=A.device)
+        beta = 0.0
+    else:
+        C = C if batched else C.unsqueeze(0)
+    need = lib.agb_cgemm_tc_workspace(bat, M, N, K)
+    ws = workspace(need, A.device, "gemm_tc")
+    st = ctypes.c_int(0)
+    al, be = complex(alpha), complex(beta)
+    check(lib.agb_cgemm_tc(opA.encode(), opB.encode(), bat, M, N, K, ptr(A2), ca, ra * ca, ptr(B2), cb, rb * cb,
+                           ptr(C), N, M * N, al.real, al.imag, be.real, be.imag, ptr(ws), ws.numel(),
+                           ctypes.byref(st), stream_ptr(A.device)), "cgemm_tc")
+    return C if batched else C[0]

@@ -161,6 +161,19 @@ int agb_prof_begin(int capacity);
 long long agb_launch_count(void);
 int agb_prof_end(double* ms_per_stage, int* marks_per_stage, int nstages);
 
+/* Batched complex64 GEMM on the tcgen05 tensor cores (3xTF32 split precision,
+ * TMA-fed), strided batch: C[b] = alpha op(A[b]) op(B[b]) + beta C[b].
+ * Replaces the torch/cuBLAS complex matmuls of the reference path
+ * (mps_complex.py:359-366, mps_pytorch.py:300-352, mpo_ops.py:1145).
+ * ws: agb_cgemm_tc_workspace(batch, M, N, K) bytes.  If status_host is not
+ * NULL the call synchronises the stream and returns the device status
+ * (AGB_ERR_TIMEOUT if a bounded wait expired). */
+size_t agb_cgemm_tc_workspace(int batch, int M, int N, int K);
+int agb_cgemm_tc(char opA, char opB, int batch, int M, int N, int K, const void* A, int64_t lda,
+                 int64_t strideA, const void* B, int64_t ldb, int64_t strideB, void* C, int64_t ldc,
+                 int64_t strideC, float alpha_re, float alpha_im, float beta_re, float beta_im, void* ws,
+                 size_t ws_bytes, int* status_host, void* stream);
+
 /* Batched complex GEMM (SIMT reference-free kernel, used by the host layer):
  * C[b] = alpha * op(A[b]) op(B[b]) + beta * C[b]; op: 'N','T','C'. */
 int agb_cgemm_batched(int dtype, char opA, char opB, int batch, int M, int N, int K,

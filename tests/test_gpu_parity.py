@@ -65,6 +65,21 @@ def test_cgemm_ops(opA, opB):
     assert rel(C, ref) < 1e-5
 
 
+@pytest.mark.parametrize("opA,opB,M,N,K,batch", [("N", "N", 70, 45, 129, 1), ("C", "N", 256, 256, 512, 3),
+                                                  ("N", "C", 128, 64, 32, 2), ("T", "T", 200, 130, 77, 1),
+                                                  ("N", "N", 512, 272, 512, 4)])
+def test_cgemm_tensor_cores_3xtf32(opA, opB, M, N, K, batch):
+    """tcgen05 3xTF32 complex GEMM against float64 numpy: FP32-class relative error
+    (<= 1e-6 + 2e-9 K: the tensor core's fp32 accumulation error grows with K)."""
+    g = torch.Generator().manual_seed(M + N + K)
+    A = crandn(batch, *((M, K) if opA == "N" else (K, M)), gen=g)
+    B = crandn(batch, *((K, N) if opB == "N" else (N, K)), gen=g)
+    C = ops.cgemm_tc(A.to(DEV), B.to(DEV), opA, opB).cpu().numpy()
+    f = {"N": lambda x: x, "T": lambda x: np.swapaxes(x, -1, -2), "C": lambda x: np.swapaxes(x, -1, -2).conj()}
+    ref = f[opA](A.numpy().astype(np.complex128)) @ f[opB](B.numpy().astype(np.complex128))
+    assert rel(C, ref) < 1e-6 + 2e-9 * K
+
+
 def _hermitian_cases():
     g = torch.Generator().manual_seed(11)
     cases = []
