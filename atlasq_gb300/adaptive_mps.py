@@ -15,6 +15,7 @@ that a caller can observe are documented where they occur:
   reference's left-to-right sampler is only correct on a right-canonical MPS,
   mps_pytorch.py:154-355) and draws Philox4x32-10 uniforms.
 """
+import ctypes
 import math
 import time
 from dataclasses import dataclass
@@ -238,11 +239,13 @@ class AdaptiveMPS:
                                 dtype=str(r["dtype"]), ms_elapsed=elapsed, condS=r["condS"])
 
     def _run_pipeline(self, gates, dt, ells):
-        """One batched launch sequence: plan -> run -> read ranks -> finalize."""
+        """One batched launch sequence: plan -> run -> read ranks -> finalize.
+        Descriptor rows are built and read with NumPy; the two small copies per
+        batch (descriptors up, results down) are the only host synchronisation."""
         lib = _lib.load()
         code = dtype_code(dt)
         G = len(gates)
-        desc = torch.zeros(G, _lib.D_NFIELDS, dtype=torch.int64)
+        desc = np.zeros((G, _lib.D_NFIELDS), dtype=np.int64)
         keep = []
         if all(U.device == self.device for _, U in gates):
             Us = torch.stack([U.to(dtype=dt) for _, U in gates]).contiguous()
@@ -250,8 +253,11 @@ class AdaptiveMPS:
             Us = torch.stack([U.to(dtype=dt, device="cpu") for _, U in gates]).contiguous()
             Us = Us.to(self.device, non_blocking=True)
         keep.append(Us)
+        u_base, u_stride = Us.data_ptr(), 16 * Us.element_size()
         maxL = maxM = maxR = 1
         meta = []
+        eps_bits = _dbits(self.eps_bond)
+        seed0 = (self._seed * 1000003 + self._operation_counter) & 0x3FFFFFFFFFFFFFFF
         for g, (i, _) in enumerate(gates):
             A = self._tensors[i]
             B = self._tensors[i + 1]
@@ -265,22 +271,25 @@ class AdaptiveMPS:
             row = desc[g]
             row[_lib.D_A] = A.data_ptr()
             row[_lib.D_B] = B.data_ptr()
-            row[_lib.D_U] = Us[g].data_ptr()
-            row[_lib.D_CHIL], row[_lib.D_CHIM], row[_lib.D_CHIR] = chiL, chiM, chiR
+            row[_lib.D_U] = u_base + g * u_stride
+            row[_lib.D_CHIL] = chiL
+            row[_lib.D_CHIM] = chiM
+            row[_lib.D_CHIR] = chiR
             row[_lib.D_CAP] = self.chi_max_per_bond[i]
-            row[_lib.D_EPS] = _dbits(self.eps_bond)
+            row[_lib.D_EPS] = eps_bits
             row[_lib.D_ELL] = int(ells[g]) if ells is not None else 0
-            row[_lib.D_SEED] = (self._seed * 1000003 + self._operation_counter + g) & 0x7FFFFFFFFFFFFFFF
+            row[_lib.D_SEED] = seed0 + g
             meta.append((i, chiL, chiM, chiR))
         wsz = _lib.SZ(0)
-        check(lib.agb_two_site_plan(code, G, ptr(desc), wsz), "two_site_plan")
+        check(lib.agb_two_site_plan(code, G, desc.ctypes.data_as(ctypes.c_void_p), ctypes.byref(wsz)),
+              "two_site_plan")
         maxell = int(desc[:, _lib.D_ELL].max())
         ws = ops.workspace(wsz.value, self.device, "two_site")
-        desc_dev = desc.to(self.device)
+        desc_dev = torch.from_numpy(desc).to(self.device)
         stream = stream_ptr(self.device)
         check(lib.agb_two_site_run(code, G, ptr(desc_dev), ptr(desc_dev), maxL, maxM, maxR, maxell,
                                    ptr(ws), wsz.value, stream), "two_site_run")
-        out = desc_dev.cpu()
+        out = desc_dev.cpu().numpy()
         res = []
         maxk = 1
         for g, (i, chiL, chiM, chiR) in enumerate(meta):
@@ -300,20 +309,20 @@ class AdaptiveMPS:
                     kk -= 1
                 if kk != k:
                     r["k"] = k = kk
-                    out[g, _lib.D_K] = kk
+                    row[_lib.D_K] = kk
             if st == _lib.AGB_OK:
                 A_new = torch.empty(chiL, 2, k, dtype=dt, device=self.device)
                 B_new = torch.empty(k, 2, chiR, dtype=dt, device=self.device)
-                out[g, _lib.D_ANEW] = A_new.data_ptr()
-                out[g, _lib.D_BNEW] = B_new.data_ptr()
+                row[_lib.D_ANEW] = A_new.data_ptr()
+                row[_lib.D_BNEW] = B_new.data_ptr()
                 r["A"], r["B"] = A_new, B_new
                 maxk = max(maxk, k)
             else:
-                out[g, _lib.D_K] = 0
-                out[g, _lib.D_ANEW] = 0
-                out[g, _lib.D_BNEW] = 0
+                row[_lib.D_K] = 0
+                row[_lib.D_ANEW] = 0
+                row[_lib.D_BNEW] = 0
             res.append(r)
-        desc_dev.copy_(out)
+        desc_dev.copy_(torch.from_numpy(out))
         check(lib.agb_two_site_finalize(code, G, ptr(desc_dev), maxL, maxR, maxk, ptr(ws), stream),
               "two_site_finalize")
         return res

@@ -77,6 +77,33 @@ template <typename T> AGB_DEV T block_sum(T v, T* red) {
   return r;
 }
 
+// Block-wide sum of two values at once (one reduction round instead of two).
+template <typename T> AGB_DEV void block_sum2(T& a, T& b, T* red /* >= 64 entries */) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  a = warp_sum(a);
+  b = warp_sum(b);
+  __syncthreads();
+  if (lane == 0) {
+    red[wid] = a;
+    red[32 + wid] = b;
+  }
+  __syncthreads();
+  if (wid == 0) {
+    T x = (lane < nw) ? red[lane] : T(0);
+    T y = (lane < nw) ? red[32 + lane] : T(0);
+    x = warp_sum(x);
+    y = warp_sum(y);
+    if (lane == 0) {
+      red[0] = x;
+      red[32] = y;
+    }
+  }
+  __syncthreads();
+  a = red[0];
+  b = red[32];
+  __syncthreads();
+}
+
 // ---------------------------------------------------------------- Philox4x32-10
 // Salmon, Moraes, Dror, Shaw, SC'11 (Random123).  Same definition as the CPU
 // oracle: ten rounds, multipliers 0xD2511F53 / 0xCD9E8D57, Weyl increments

@@ -49,7 +49,7 @@ __global__ void __launch_bounds__(512, 1) tridiag_cluster_kernel(const HeevdProb
   CX* wprev = vprev + n;
   CX* rows = wprev + n;
   __shared__ R normp[8];
-  __shared__ R red[32];
+  __shared__ R red[64];
   __shared__ CX sc[4];
   __shared__ R mxp[8];
   CX* H = (CX*)P.H;
@@ -145,38 +145,42 @@ __global__ void __launch_bounds__(512, 1) tridiag_cluster_kernel(const HeevdProb
     }
     __syncthreads();
     // ---------------- B: fused previous update + partial matvec over own rows
+    // Row pass (warp per row): apply the pending rank-2 update of the previous
+    // step to columns > j and accumulate sum_{c <= r} A[r][c] v_c.
     {
       const int i0 = (j + 1 - q + C - 1) / C > 0 ? (j + 1 - q + C - 1) / C : 0;
       for (int i = i0 + wid; i < nown; i += nw) {
         const int r = q + i * C;
         CX* row = rows + row_offset(i, q, C);
-        const CX vr = vprev[r], wr = wprev[r], vjr = v[r];
+        const CX vr = vprev[r], wr = wprev[r];
         CX acc = czero<CX>();
         for (int c = j + 1 + lane; c <= r; c += 32) {
           CX a = row[c];
-          if (prev_active && c >= j + 1 && j >= 1) {
-            // column j (== previous j+1) was updated at the end of the previous step
-            if (c > j) {
-              a = csub(a, cmul(vr, cconj(wprev[c])));
-              a = csub(a, cmul(wr, cconj(vprev[c])));
-              row[c] = a;
-            }
+          if (prev_active) {  // column j itself was updated at the end of the previous step
+            a = csub(a, cmul(vr, cconj(wprev[c])));
+            a = csub(a, cmul(wr, cconj(vprev[c])));
+            row[c] = a;
           }
-          if (active) {
-            cfma(acc, a, v[c]);
-            if (c < r) {
-              const CX contrib = cmulc(a, vjr);  // conj(A[r][c]) * v_r
-              atomicAdd(&pp[c].x, contrib.x);
-              atomicAdd(&pp[c].y, contrib.y);
-            }
-          }
+          if (active) cfma(acc, a, v[c]);
         }
         if (active) {
           acc = warp_csum(acc);
-          if (lane == 0) {
-            atomicAdd(&pp[r].x, acc.x);
-            atomicAdd(&pp[r].y, acc.y);
+          if (lane == 0) pp[r] = acc;  // rows are owned by one warp: plain store
+        }
+      }
+      __syncthreads();
+      // Column pass (thread per column): the strictly-lower entries of the own
+      // rows contribute conj(A[r][c]) v_r to p[c] through Hermitian symmetry.
+      // No atomics: one thread owns each column.
+      if (active) {
+        for (int c = j + 1 + tid; c < n; c += nt) {
+          const int ic = (c + 1 - q + C - 1) / C > 0 ? (c + 1 - q + C - 1) / C : 0;  // own rows r > c
+          CX acc = czero<CX>();
+          for (int i = (ic > i0 ? ic : i0); i < nown; ++i) {
+            const int r = q + i * C;
+            cfma(acc, cconj(rows[row_offset(i, q, C) + c]), v[r]);
           }
+          pp[c] = cadd(pp[c], acc);
         }
       }
     }
@@ -190,8 +194,8 @@ __global__ void __launch_bounds__(512, 1) tridiag_cluster_kernel(const HeevdProb
       w[r] = pr;
       cfmac(kpart, pr, v[r]);
     }
-    const R kr = block_sum(kpart.x, red);
-    const R ki = block_sum(kpart.y, red);
+    R kr = kpart.x, ki = kpart.y;
+    block_sum2(kr, ki, red);
     const CX K = cscale(cmul(t, mk<CX>(kr, ki)), R(-0.5));
     for (int r = j + 1 + tid; r < n; r += nt) w[r] = cadd(w[r], cmul(K, v[r]));
     __syncthreads();
@@ -236,10 +240,13 @@ size_t tridiag_cluster_smem(int esz, int n, int C) {
   return (best + 6 * (size_t)n) * esz;
 }
 
-// Pick the smallest power-of-two cluster whose shared memory fits; 0 if none.
+// Pick the cluster size (1..8 CTAs) for a matrix of size n.
 int tridiag_cluster_size(int esz, int n) {
-  for (int C = 1; C <= 8; C *= 2)
-    if (tridiag_cluster_smem(esz, n, C) <= 200 * 1024) return C;
+  // The per-step work (not the barriers) dominates for n > 256, so large
+  // matrices take the largest portable cluster.
+  const int lo = n > 256 ? 8 : 1;
+  for (int C = lo; C <= 8; ++C)
+    if (tridiag_cluster_smem(esz, n, C) <= 224 * 1024) return C;
   return 0;
 }
 
