@@ -3,11 +3,14 @@ ATLAS-Q AdaptiveMPS API (followthesapper/ATLAS-Q 0.7.0).
 
 Public names mirror the reference: AdaptiveMPS, DTypePolicy, robust_svd,
 robust_qr, choose_rank_from_sigma, MPO, MPOBuilder, expectation_value,
-correlation_function, MPSStatistics, get_adaptive_mps()."""
+correlation_function, MPSStatistics, get_adaptive_mps().  Additions for the
+GB300 path: MPSBatch (many instances per launch sequence) and
+rank_predictor.RankPredictor (learned kept-rank sizing)."""
 
 __version__ = "0.1.0"
 
-from .adaptive_mps import AdaptiveMPS, DTypePolicy  # noqa: E402
+from .adaptive_mps import AdaptiveMPS, DTypePolicy, apply_gate_entries  # noqa: E402
+from .batched import MPSBatch  # noqa: E402
 from .diagnostics import MPSStatistics, bond_entropy_from_S, effective_rank, spectral_gap  # noqa: E402
 from .linalg_robust import condition_number, robust_qr, robust_svd  # noqa: E402
 from .mpo_ops import (MPO, MPOBuilder, correlation_function, expectation_value,  # noqa: E402

@@ -30,6 +30,8 @@ D_ANEW, D_BNEW, D_ELL, D_SEED, D_WS = 8, 9, 10, 11, 12
 D_K, D_EPSLOC, D_ENTROPY, D_CONDS, D_STATUS, D_TOTAL, D_NEEDED, D_MODE = 16, 17, 18, 19, 20, 21, 22, 23
 D_NFIELDS = 32
 
+MLP_NPARAM = 8769
+
 STAGES = ["host_gap", "setup", "contract", "gram", "tridiag", "bisect", "invit", "cluster",
           "backtransform", "polish", "xv", "rank", "scatter"]
 
@@ -60,6 +62,7 @@ _SIGS = {
     "agb_two_site_run": (I, [I, I, P, P, I, I, I, I, P, SZ, P]),
     "agb_two_site_finalize": (I, [I, I, P, I, I, I, P, P]),
     "agb_single_qubit_gate": (I, [I, P, P, I, I, P]),
+    "agb_single_qubit_batch": (I, [I, I, P, I, P]),
     "agb_heevd_workspace": (SZ, [I, I, I]),
     "agb_heevd": (I, [I, I, I, I, P, P, P, P, SZ, U64, P]),
     "agb_qr_workspace": (SZ, [I, I, I]),
@@ -71,6 +74,10 @@ _SIGS = {
     "agb_prof_begin": (I, [I]),
     "agb_launch_count": (ctypes.c_longlong, []),
     "agb_prof_end": (I, [P, P, I]),
+    "agb_mlp_forward": (I, [P, P, I, P, P]),
+    "agb_mlp_backward": (I, [P, P, P, I, P, P, P]),
+    "agb_mlp_adam": (I, [P, P, P, P, I, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                         ctypes.c_float, P]),
     "agb_cgemm_tc_workspace": (SZ, [I, I, I, I]),
     "agb_cgemm_tc": (I, [ctypes.c_char, ctypes.c_char, I, I, I, I, P, I64, I64, P, I64, I64, P, I64, I64,
                          ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, P, SZ, P, P]),

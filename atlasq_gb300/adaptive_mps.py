@@ -76,7 +76,13 @@ class AdaptiveMPS:
         self._seed = int(seed)
         self._pending = []
         self._pending_sites = set()
-        self.rank_predictor = None  # optional callable(mps, list_of_bonds) -> list of ell
+        self._pending_1q = []        # queued single-qubit gates (site, U) in order
+        # optional callable(mps, [(bond, U4x4), ...]) -> list of ell (eigenpairs to compute per gate)
+        self.rank_predictor = None
+        self.feature_log = None      # list -> (features, k, full) per gate is appended (predictor training data)
+        self._last_entropy = {}      # bond -> entanglement entropy at its last update
+        self.rank_fallbacks = 0      # gates re-run at full size after a too-small predicted ell
+        self.ell_total = 0           # eigenpairs computed, summed over gates (fallback runs included)
         self.batch_log = []          # per-flush (n_gates, seconds) for profiling
         self._initialize_zero_state(bond_dim)
 
@@ -111,6 +117,10 @@ class AdaptiveMPS:
         self.is_canonical = True
 
     def _flush(self):
+        if self._pending_1q:
+            g1 = self._pending_1q
+            self._pending_1q = []
+            apply_single_qubit_entries([(self, q, U) for q, U in g1])
         if self._pending:
             gates = self._pending
             self._pending = []
@@ -164,16 +174,15 @@ class AdaptiveMPS:
     # ------------------------------------------------------------ gates
     @torch.no_grad()
     def apply_single_qubit_gate(self, q: int, U2: torch.Tensor):
-        """adaptive_mps.py:159-180; applies U^T like the reference."""
+        """adaptive_mps.py:159-180; applies U^T like the reference.  Queued: all
+        queued single-qubit gates run in one launch at the next flush, before the
+        queued two-site gates (a single-qubit gate on a site with a queued
+        two-site gate flushes first, so the order of operations is kept)."""
         assert 0 <= q < self.num_qubits, f"Qubit index {q} out of range"
         assert U2.shape == (2, 2), "U2 must be 2x2"
         if q in self._pending_sites:
             self._flush()
-        T = self._tensors[q]
-        if not T.is_contiguous():
-            T = T.contiguous()
-        ops.single_qubit_gate_(T, U2)
-        self._tensors[q] = T
+        self._pending_1q.append((q, U2))
         self.is_canonical = False
 
     @torch.no_grad()
@@ -206,126 +215,7 @@ class AdaptiveMPS:
         return ok
 
     def _apply_batch(self, gates):
-        t0 = time.perf_counter()
-        dt = self.dtype_policy.default
-        ells = None
-        if self.rank_predictor is not None:
-            ells = self.rank_predictor(self, [i for i, _ in gates])
-        res = self._run_pipeline(gates, dt, ells)
-        # rank fallback: predicted sketch too small -> rerun those gates at full size
-        redo = [g for g, r in enumerate(res) if r["status"] == _lib.AGB_ERR_RANK]
-        if redo:
-            full = self._run_pipeline([gates[g] for g in redo], dt, None)
-            for g, r in zip(redo, full):
-                r["driver"] = "gb300_gram_heevd_full"
-                res[g] = r
-        # precision promotion (adaptive_mps.py:268-274)
-        thr = self.dtype_policy.promote_if_cond_gt
-        for g, r in enumerate(res):
-            if math.isfinite(r["condS"]) and r["condS"] > thr and dt != _C128:
-                r2 = self._run_pipeline([gates[g]], _C128, None)[0]
-                r2["driver"] = "gb300_gram_heevd_c128"
-                res[g] = r2
-        elapsed = (time.perf_counter() - t0) * 1000.0 / max(1, len(gates))
-        self.batch_log.append((len(gates), elapsed * len(gates) / 1000.0))
-        for (i, _), r in zip(gates, res):
-            self._tensors[i] = r["A"]
-            self._tensors[i + 1] = r["B"]
-            self._bond_dims[i] = r["k"]
-            if not check_entropy_sanity(r["entropy"], r["chiL"], r["chiR"]):
-                print(f"Warning: Entropy {r['entropy']:.3f} exceeds physical bound at bond {i}")
-            self._log_operation(bond=i, k_star=r["k"], chi_before=r["chiM"], chi_after=r["k"],
-                                eps_local=r["eps_local"], entropy=r["entropy"], svd_driver=r["driver"],
-                                dtype=str(r["dtype"]), ms_elapsed=elapsed, condS=r["condS"])
-
-    def _run_pipeline(self, gates, dt, ells):
-        """One batched launch sequence: plan -> run -> read ranks -> finalize.
-        Descriptor rows are built and read with NumPy; the two small copies per
-        batch (descriptors up, results down) are the only host synchronisation."""
-        lib = _lib.load()
-        code = dtype_code(dt)
-        G = len(gates)
-        desc = np.zeros((G, _lib.D_NFIELDS), dtype=np.int64)
-        keep = []
-        if all(U.device == self.device for _, U in gates):
-            Us = torch.stack([U.to(dtype=dt) for _, U in gates]).contiguous()
-        else:
-            Us = torch.stack([U.to(dtype=dt, device="cpu") for _, U in gates]).contiguous()
-            Us = Us.to(self.device, non_blocking=True)
-        keep.append(Us)
-        u_base, u_stride = Us.data_ptr(), 16 * Us.element_size()
-        maxL = maxM = maxR = 1
-        meta = []
-        eps_bits = _dbits(self.eps_bond)
-        seed0 = (self._seed * 1000003 + self._operation_counter) & 0x3FFFFFFFFFFFFFFF
-        for g, (i, _) in enumerate(gates):
-            A = self._tensors[i]
-            B = self._tensors[i + 1]
-            if A.dtype != dt or not A.is_contiguous():
-                A = A.to(dt).contiguous()
-            if B.dtype != dt or not B.is_contiguous():
-                B = B.to(dt).contiguous()
-            keep += [A, B]
-            chiL, chiM, chiR = A.shape[0], A.shape[2], B.shape[2]
-            maxL, maxM, maxR = max(maxL, chiL), max(maxM, chiM), max(maxR, chiR)
-            row = desc[g]
-            row[_lib.D_A] = A.data_ptr()
-            row[_lib.D_B] = B.data_ptr()
-            row[_lib.D_U] = u_base + g * u_stride
-            row[_lib.D_CHIL] = chiL
-            row[_lib.D_CHIM] = chiM
-            row[_lib.D_CHIR] = chiR
-            row[_lib.D_CAP] = self.chi_max_per_bond[i]
-            row[_lib.D_EPS] = eps_bits
-            row[_lib.D_ELL] = int(ells[g]) if ells is not None else 0
-            row[_lib.D_SEED] = seed0 + g
-            meta.append((i, chiL, chiM, chiR))
-        wsz = _lib.SZ(0)
-        check(lib.agb_two_site_plan(code, G, desc.ctypes.data_as(ctypes.c_void_p), ctypes.byref(wsz)),
-              "two_site_plan")
-        maxell = int(desc[:, _lib.D_ELL].max())
-        ws = ops.workspace(wsz.value, self.device, "two_site")
-        desc_dev = torch.from_numpy(desc).to(self.device)
-        stream = stream_ptr(self.device)
-        check(lib.agb_two_site_run(code, G, ptr(desc_dev), ptr(desc_dev), maxL, maxM, maxR, maxell,
-                                   ptr(ws), wsz.value, stream), "two_site_run")
-        out = desc_dev.cpu().numpy()
-        res = []
-        maxk = 1
-        for g, (i, chiL, chiM, chiR) in enumerate(meta):
-            row = out[g]
-            st = int(row[_lib.D_STATUS])
-            k = int(row[_lib.D_K])
-            r = {"status": st, "k": k, "eps_local": _bitsd(int(row[_lib.D_EPSLOC])),
-                 "entropy": _bitsd(int(row[_lib.D_ENTROPY])), "condS": _bitsd(int(row[_lib.D_CONDS])),
-                 "chiL": chiL, "chiM": chiM, "chiR": chiR, "driver": "gb300_gram_heevd", "dtype": dt,
-                 "mode": int(row[_lib.D_MODE]), "ell": int(row[_lib.D_ELL])}
-            if st not in (_lib.AGB_OK, _lib.AGB_ERR_RANK):
-                check(st, f"two-site update on bond {i}")
-            ok = self._budget_ok_fn(chiL, chiM, chiR, dt)
-            if ok is not None and st == _lib.AGB_OK:
-                kk = k
-                while kk > 1 and not ok(kk):
-                    kk -= 1
-                if kk != k:
-                    r["k"] = k = kk
-                    row[_lib.D_K] = kk
-            if st == _lib.AGB_OK:
-                A_new = torch.empty(chiL, 2, k, dtype=dt, device=self.device)
-                B_new = torch.empty(k, 2, chiR, dtype=dt, device=self.device)
-                row[_lib.D_ANEW] = A_new.data_ptr()
-                row[_lib.D_BNEW] = B_new.data_ptr()
-                r["A"], r["B"] = A_new, B_new
-                maxk = max(maxk, k)
-            else:
-                row[_lib.D_K] = 0
-                row[_lib.D_ANEW] = 0
-                row[_lib.D_BNEW] = 0
-            res.append(r)
-        desc_dev.copy_(torch.from_numpy(out))
-        check(lib.agb_two_site_finalize(code, G, ptr(desc_dev), maxL, maxR, maxk, ptr(ws), stream),
-              "two_site_finalize")
-        return res
+        apply_gate_entries([(self, i, U) for i, U in gates])
 
     # ------------------------------------------------------------ canonical forms
     def _common(self, T):
@@ -532,3 +422,232 @@ class AdaptiveMPS:
 
     def swap(self, q0, q1):
         self._two(q0, q1, [[1, 0, 0, 0], [0, 0, 1, 0], [0, 1, 0, 0], [0, 0, 0, 1]], False)
+
+
+# ---------------------------------------------------------------- batched single-qubit gates
+def apply_single_qubit_entries(entries):
+    """Apply queued single-qubit gates ``[(mps, site, U2), ...]`` (any number of
+    instances, in order per site) with one launch of agb_single_qubit_batch."""
+    if not entries:
+        return
+    lib = _lib.load()
+    device = entries[0][0].device
+    groups = {}
+    for m, q, U in entries:
+        if m.device != device:
+            raise ValueError("batched entries must share the device")
+        groups.setdefault((id(m), q), (m, q, []))[2].append(U)
+    dts = {m._tensors[q].dtype for m, q, _ in groups.values()}
+    if len(dts) != 1:
+        for dt in dts:  # one launch per tensor dtype
+            apply_single_qubit_entries([e for e in entries if e[0]._tensors[e[1]].dtype == dt])
+        return
+    dt = dts.pop()
+    if len(groups) > 65535:
+        keys = list(groups)
+        for c in range(0, len(keys), 65535):
+            part = set(keys[c:c + 65535])
+            apply_single_qubit_entries([e for e in entries if (id(e[0]), e[1]) in part])
+        return
+    ng = len(groups)
+    nu = len(entries)
+    desc = np.zeros(ng * 5 + nu, dtype=np.int64)
+    keep = []
+    host_U, host_slot = [], []
+    first = 0
+    max_elems = 1
+    for g, (m, q, Us) in enumerate(groups.values()):
+        T = m._tensors[q]
+        if not T.is_contiguous():
+            T = T.contiguous()
+            m._tensors[q] = T
+        keep.append(T)
+        desc[5 * g:5 * g + 5] = (T.data_ptr(), T.shape[0], T.shape[2], first, len(Us))
+        max_elems = max(max_elems, T.shape[0] * T.shape[2])
+        for j, U in enumerate(Us):
+            if U.device == device and U.dtype == dt and U.is_contiguous():
+                keep.append(U)
+                desc[ng * 5 + first + j] = U.data_ptr()
+            else:
+                host_U.append(U.detach().to("cpu", dt))
+                host_slot.append(ng * 5 + first + j)
+        first += len(Us)
+    if host_U:
+        Ud = torch.stack(host_U).to(device)
+        keep.append(Ud)
+        es = 4 * Ud.element_size()
+        for j, slot in enumerate(host_slot):
+            desc[slot] = Ud.data_ptr() + j * es
+    desc_dev = torch.from_numpy(desc).to(device, non_blocking=False)
+    check(lib.agb_single_qubit_batch(dtype_code(dt), ng, ptr(desc_dev), max_elems, stream_ptr(device)),
+          "single_qubit_batch")
+    # buffers released here return to the stream-ordered caching allocator, so
+    # they are not reused before this launch has consumed them
+    del keep
+
+
+# ---------------------------------------------------------------- batched two-site updates
+def apply_gate_entries(entries):
+    """Apply queued two-site gates ``[(mps, bond, U4), ...]`` as one batched
+    launch sequence.  Entries may come from many AdaptiveMPS instances (of any
+    sizes); within one instance their bonds must be disjoint.  Per instance the
+    result, the statistics and the rank-fallback / precision-promotion rules
+    are exactly those of applying its gates alone (adaptive_mps.py:182-308)."""
+    if not entries:
+        return
+    t0 = time.perf_counter()
+    mps0 = entries[0][0]
+    dt = mps0.dtype_policy.default
+    device = mps0.device
+    for m, _, _ in entries:
+        if m.dtype_policy.default != dt or m.device != device:
+            raise ValueError("batched entries must share the dtype policy and the device")
+    # group positions per instance (predictor and feature hooks see one instance at a time)
+    groups = {}
+    for g, (m, i, U) in enumerate(entries):
+        groups.setdefault(id(m), (m, []))[1].append(g)
+    ells = None
+    feats = {}
+    for m, idx in groups.values():
+        if m.feature_log is not None:
+            from .rank_predictor import gate_features
+            feats[id(m)] = (idx, gate_features(m, [(entries[g][1], entries[g][2]) for g in idx]))
+        if m.rank_predictor is not None:
+            if ells is None:
+                ells = [0] * len(entries)
+            pe = m.rank_predictor(m, [(entries[g][1], entries[g][2]) for g in idx])
+            for g, e in zip(idx, pe):
+                ells[g] = int(e)
+    res = _run_pipeline(entries, dt, ells)
+    for m, idx in groups.values():
+        m.ell_total += sum(res[g]["ell"] for g in idx)
+    # rank fallback: predicted size too small -> rerun those gates at full size
+    redo = [g for g, r in enumerate(res) if r["status"] == _lib.AGB_ERR_RANK]
+    if redo:
+        full = _run_pipeline([entries[g] for g in redo], dt, None)
+        for g, r in zip(redo, full):
+            r["driver"] = "gb300_gram_heevd_full"
+            res[g] = r
+            entries[g][0].rank_fallbacks += 1
+            entries[g][0].ell_total += r["ell"]
+    # precision promotion (adaptive_mps.py:268-274)
+    promote = [g for g, r in enumerate(res)
+               if math.isfinite(r["condS"]) and r["condS"] > entries[g][0].dtype_policy.promote_if_cond_gt
+               and dt != _C128]
+    if promote:
+        r2 = _run_pipeline([entries[g] for g in promote], _C128, None)
+        for g, r in zip(promote, r2):
+            r["driver"] = "gb300_gram_heevd_c128"
+            res[g] = r
+    elapsed = (time.perf_counter() - t0) * 1000.0 / len(entries)
+    for m, idx in groups.values():
+        m.batch_log.append((len(idx), elapsed * len(idx) / 1000.0))
+        fi = feats.get(id(m))
+        for j, g in enumerate(idx):
+            _, i, _ = entries[g]
+            r = res[g]
+            m._tensors[i] = r["A"]
+            m._tensors[i + 1] = r["B"]
+            m._bond_dims[i] = r["k"]
+            m._last_entropy[i] = r["entropy"]
+            if fi is not None:
+                m.feature_log.append((fi[1][0][j], r["k"], int(fi[1][1][j])))
+            if not check_entropy_sanity(r["entropy"], r["chiL"], r["chiR"]):
+                print(f"Warning: Entropy {r['entropy']:.3f} exceeds physical bound at bond {i}")
+            m._log_operation(bond=i, k_star=r["k"], chi_before=r["chiM"], chi_after=r["k"],
+                             eps_local=r["eps_local"], entropy=r["entropy"], svd_driver=r["driver"],
+                             dtype=str(r["dtype"]), ms_elapsed=elapsed, condS=r["condS"])
+
+
+def _run_pipeline(entries, dt, ells):
+    """One batched launch sequence: plan -> run -> read ranks -> finalize.
+    Descriptor rows are built and read with NumPy; the two small copies per
+    batch (descriptors up, results down) are the only host synchronisation."""
+    lib = _lib.load()
+    code = dtype_code(dt)
+    device = entries[0][0].device
+    G = len(entries)
+    desc = np.zeros((G, _lib.D_NFIELDS), dtype=np.int64)
+    keep = []
+    if all(U.device == device for _, _, U in entries):
+        Us = torch.stack([U.to(dtype=dt) for _, _, U in entries]).contiguous()
+    else:
+        Us = torch.stack([U.to(dtype=dt, device="cpu") for _, _, U in entries]).contiguous()
+        Us = Us.to(device, non_blocking=True)
+    keep.append(Us)
+    u_base, u_stride = Us.data_ptr(), 16 * Us.element_size()
+    maxL = maxM = maxR = 1
+    meta = []
+    seeds = {}
+    for g, (m, i, _) in enumerate(entries):
+        A = m._tensors[i]
+        B = m._tensors[i + 1]
+        if A.dtype != dt or not A.is_contiguous():
+            A = A.to(dt).contiguous()
+        if B.dtype != dt or not B.is_contiguous():
+            B = B.to(dt).contiguous()
+        keep += [A, B]
+        chiL, chiM, chiR = A.shape[0], A.shape[2], B.shape[2]
+        maxL, maxM, maxR = max(maxL, chiL), max(maxM, chiM), max(maxR, chiR)
+        # per-instance sketch seed: (instance seed, operation counter, position in its batch)
+        j = seeds.get(id(m), 0)
+        seeds[id(m)] = j + 1
+        seed = ((m._seed * 1000003 + m._operation_counter) & 0x3FFFFFFFFFFFFFFF) + j
+        row = desc[g]
+        row[_lib.D_A] = A.data_ptr()
+        row[_lib.D_B] = B.data_ptr()
+        row[_lib.D_U] = u_base + g * u_stride
+        row[_lib.D_CHIL] = chiL
+        row[_lib.D_CHIM] = chiM
+        row[_lib.D_CHIR] = chiR
+        row[_lib.D_CAP] = m.chi_max_per_bond[i]
+        row[_lib.D_EPS] = _dbits(m.eps_bond)
+        row[_lib.D_ELL] = int(ells[g]) if ells is not None else 0
+        row[_lib.D_SEED] = seed
+        meta.append((m, i, chiL, chiM, chiR))
+    wsz = _lib.SZ(0)
+    check(lib.agb_two_site_plan(code, G, desc.ctypes.data_as(ctypes.c_void_p), ctypes.byref(wsz)),
+          "two_site_plan")
+    maxell = int(desc[:, _lib.D_ELL].max())
+    ws = ops.workspace(wsz.value, device, "two_site")
+    desc_dev = torch.from_numpy(desc).to(device)
+    stream = stream_ptr(device)
+    check(lib.agb_two_site_run(code, G, ptr(desc_dev), ptr(desc_dev), maxL, maxM, maxR, maxell,
+                               ptr(ws), wsz.value, stream), "two_site_run")
+    out = desc_dev.cpu().numpy()
+    res = []
+    maxk = 1
+    for g, (m, i, chiL, chiM, chiR) in enumerate(meta):
+        row = out[g]
+        st = int(row[_lib.D_STATUS])
+        k = int(row[_lib.D_K])
+        r = {"status": st, "k": k, "eps_local": _bitsd(int(row[_lib.D_EPSLOC])),
+             "entropy": _bitsd(int(row[_lib.D_ENTROPY])), "condS": _bitsd(int(row[_lib.D_CONDS])),
+             "chiL": chiL, "chiM": chiM, "chiR": chiR, "driver": "gb300_gram_heevd", "dtype": dt,
+             "mode": int(row[_lib.D_MODE]), "ell": int(row[_lib.D_ELL])}
+        if st not in (_lib.AGB_OK, _lib.AGB_ERR_RANK):
+            check(st, f"two-site update on bond {i}")
+        ok = m._budget_ok_fn(chiL, chiM, chiR, dt)
+        if ok is not None and st == _lib.AGB_OK:
+            kk = k
+            while kk > 1 and not ok(kk):
+                kk -= 1
+            if kk != k:
+                r["k"] = k = kk
+                row[_lib.D_K] = kk
+        if st == _lib.AGB_OK:
+            A_new = torch.empty(chiL, 2, k, dtype=dt, device=device)
+            B_new = torch.empty(k, 2, chiR, dtype=dt, device=device)
+            row[_lib.D_ANEW] = A_new.data_ptr()
+            row[_lib.D_BNEW] = B_new.data_ptr()
+            r["A"], r["B"] = A_new, B_new
+            maxk = max(maxk, k)
+        else:
+            row[_lib.D_K] = 0
+            row[_lib.D_ANEW] = 0
+            row[_lib.D_BNEW] = 0
+        res.append(r)
+    desc_dev.copy_(torch.from_numpy(out))
+    check(lib.agb_two_site_finalize(code, G, ptr(desc_dev), maxL, maxR, maxk, ptr(ws), stream),
+          "two_site_finalize")
+    return res

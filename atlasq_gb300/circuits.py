@@ -62,6 +62,37 @@ def hea_circuit(n, layers, seed):
     return ops
 
 
+def rx(theta):
+    c, s = math.cos(theta / 2), math.sin(theta / 2)
+    return torch.tensor([[c, complex(0, -s)], [complex(0, -s), c]], dtype=torch.complex64)
+
+
+def rzz(theta):
+    """exp(-i theta/2 Z(x)Z) in the basis 2*q_i + q_{i+1}."""
+    m, p = complex(math.cos(theta / 2), -math.sin(theta / 2)), complex(math.cos(theta / 2), math.sin(theta / 2))
+    return torch.diag(torch.tensor([m, p, p, m], dtype=torch.complex64))
+
+
+def trotter_ising(n, steps, seed, dt_range=(0.05, 0.6)):
+    """Transverse-field Ising Trotter circuit with disordered couplings:
+    per step, RZZ(2 J_b dt) on every bond (even bonds, then odd) and RX(2 h_q dt)
+    on every qubit; J, h uniform in [0.5, 1.5], dt uniform in dt_range per step.
+    Entanglement grows at a rate set by J dt, so kept ranks sit well below the
+    full two-site size (the workload the rank predictor is meant for)."""
+    gen = torch.Generator().manual_seed(seed)
+    ops = []
+    for _ in range(steps):
+        dt = dt_range[0] + (dt_range[1] - dt_range[0]) * float(torch.rand(1, generator=gen, dtype=torch.float64))
+        J = 0.5 + torch.rand(n - 1, generator=gen, dtype=torch.float64)
+        h = 0.5 + torch.rand(n, generator=gen, dtype=torch.float64)
+        for par in (0, 1):
+            for b in range(par, n - 1, 2):
+                ops.append(("2q", b, rzz(2 * float(J[b]) * dt)))
+        for q in range(n):
+            ops.append(("1q", q, rx(2 * float(h[q]) * dt)))
+    return ops
+
+
 def layers_of(ops):
     """Split an op list into maximal runs whose two-site gates touch disjoint
     sites (single-qubit gates end a run only if they touch a pending site)."""

@@ -325,33 +325,70 @@ __global__ void __launch_bounds__(128) invit_kernel(const HeevdProb* __restrict_
   }
   for (int it = 0; it < 3; ++it) {
     const R s = R(1) / sqrt(fmax(nrm, rlim<R>::pivmin()));
-    // forward: apply P and L
+    // Forward (apply P and L) and backward substitution.  The factor and
+    // iterate loads do not depend on the recurrence, so each chunk of IB steps
+    // loads its operands into registers first and then runs the serial chain:
+    // IB loads in flight instead of one dependent load per step.  Within a
+    // chunk every load of Y precedes the store to the same element.
+    constexpr int IB = 8;
     R bi = Y[t] * s;
-    for (int i = 0; i < n - 1; ++i) {
-      R bn = Y[(i + 1) * L + t] * s;
-      if (Pv[i * L + t] != R(0)) {
-        const R tmp = bi;
-        bi = bn;
-        bn = tmp;
+    for (int i0 = 0; i0 < n - 1; i0 += IB) {
+      R yb[IB], pv[IB], lm[IB];
+#pragma unroll
+      for (int k = 0; k < IB; ++k) {
+        const int i = i0 + k;
+        if (i < n - 1) {
+          yb[k] = Y[(int64_t)(i + 1) * L + t];
+          pv[k] = Pv[(int64_t)i * L + t];
+          lm[k] = Lm[(int64_t)i * L + t];
+        }
       }
-      Y[i * L + t] = bi;
-      bi = bn - Lm[i * L + t] * bi;
+#pragma unroll
+      for (int k = 0; k < IB; ++k) {
+        const int i = i0 + k;
+        if (i < n - 1) {
+          R bn = yb[k] * s;
+          if (pv[k] != R(0)) {
+            const R tmp = bi;
+            bi = bn;
+            bn = tmp;
+          }
+          Y[(int64_t)i * L + t] = bi;
+          bi = bn - lm[k] * bi;
+        }
+      }
     }
     Y[(int64_t)(n - 1) * L + t] = bi;
-    // backward substitution
     R x1 = 0, x2 = 0;
     nrm = 0;
-    for (int i = n - 1; i >= 0; --i) {
-      R u = U0[i * L + t];
-      if (fabs(u) < piv) u = copysign(piv, u == R(0) ? R(1) : u);
-      const R x = (Y[i * L + t] - U1[i * L + t] * x1 - U2[i * L + t] * x2) / u;
-      Y[i * L + t] = x;
-      nrm += x * x;
-      x2 = x1;
-      x1 = x;
+    for (int i0 = n - 1; i0 >= 0; i0 -= IB) {
+      R u0[IB], u1[IB], u2[IB], yb[IB];
+#pragma unroll
+      for (int k = 0; k < IB; ++k) {
+        const int i = i0 - k;
+        if (i >= 0) {
+          u0[k] = U0[(int64_t)i * L + t];
+          u1[k] = U1[(int64_t)i * L + t];
+          u2[k] = U2[(int64_t)i * L + t];
+          yb[k] = Y[(int64_t)i * L + t];
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < IB; ++k) {
+        const int i = i0 - k;
+        if (i >= 0) {
+          R u = u0[k];
+          if (fabs(u) < piv) u = copysign(piv, u == R(0) ? R(1) : u);
+          const R x = (yb[k] - u1[k] * x1 - u2[k] * x2) / u;
+          Y[(int64_t)i * L + t] = x;
+          nrm += x * x;
+          x2 = x1;
+          x1 = x;
+        }
+      }
     }
     if (!(nrm < R(1e300)) || !(nrm > R(0))) {  // overflow / breakdown: restart from a unit vector
-      for (int i = 0; i < n; ++i) Y[i * L + t] = (i == (t % n)) ? R(1) : R(0);
+      for (int i = 0; i < n; ++i) Y[(int64_t)i * L + t] = (i == (t % n)) ? R(1) : R(0);
       nrm = 1;
     }
   }
@@ -683,10 +720,12 @@ int launch_heevd_values(HeevdProb* probs, int count, int maxn, int maxell, cudaS
     attr_set[esz == 16] = true;
   }
   prof_mark(AGB_ST_TRIDIAG, s);
-  if (tridiag_cluster_size(esz, maxn) > 0) {
-    const int rc0 = launch_tridiag_cluster<CX>(probs, count, maxn, s);
-    if (rc0) return rc0;
-  } else {
+  // cluster kernel (rows in distributed shared memory, overflow rows in L2);
+  // the single-CTA kernel only if the device refuses the cluster launch
+  const int rc0 = tridiag_cluster_size(esz, maxn) > 0 ? launch_tridiag_cluster<CX>(probs, count, maxn, s)
+                                                      : AGB_ERR_UNSUPPORTED;
+  if (rc0 != AGB_OK) {
+    cudaGetLastError();
     tridiag_kernel<CX><<<count, 1024, sm_tri, s>>>(probs);
     AGB_CHECK_LAUNCH();
   }

@@ -16,6 +16,13 @@
 //      column j+1 of its rows for the next reflector.
 // Outputs match the single-CTA kernel: d, e (real), tau (complex), reflector v_j
 // in row j of H (columns j+2 .. n-1, v_j[j+1] = 1 implicit), scale.
+//
+// Rows that do not fit (matrices above ~700 for complex64 at 8 CTAs) stay in
+// place in the lower triangle of H (L2-resident): a CTA keeps its first
+// `isplit` rows (the short ones) in shared memory and addresses the rest as
+// H[r][0..r].  The reflectors are written to the strictly upper part of H
+// (row j, columns >= j+2), which the overflow rows never touch.  Overflow rows
+// are read and written only by their owning CTA, between block barriers.
 #include <cooperative_groups.h>
 
 #include "heevd.cuh"
@@ -28,7 +35,8 @@ namespace {
 AGB_DEV int row_offset(int i, int q, int C) { return i * (q + 1) + C * (i * (i - 1) / 2); }
 
 template <typename CX>
-__global__ void __launch_bounds__(512, 1) tridiag_cluster_kernel(const HeevdProb* __restrict__ probs, int C) {
+__global__ void __launch_bounds__(512, 1) tridiag_cluster_kernel(const HeevdProb* __restrict__ probs, int C,
+                                                                 int cap_elems) {
   typedef typename cx_traits<CX>::R R;
   cg::cluster_group cluster = cg::this_cluster();
   const int q = (int)cluster.block_rank();
@@ -48,12 +56,18 @@ __global__ void __launch_bounds__(512, 1) tridiag_cluster_kernel(const HeevdProb
   CX* vprev = w + n;
   CX* wprev = vprev + n;
   CX* rows = wprev + n;
-  __shared__ R normp[8];
+  __shared__ R normp[16];
   __shared__ R red[64];
   __shared__ CX sc[4];
-  __shared__ R mxp[8];
+  __shared__ R mxp[16];
   CX* H = (CX*)P.H;
   const int64_t ld = P.ldh;
+  // own rows [0, isplit) are packed in shared memory, the rest live in H
+  int isplit = 0;
+  while (isplit < nown && row_offset(isplit + 1, q, C) <= cap_elems) ++isplit;
+  auto rowp = [&](int i) -> CX* {
+    return (i < isplit) ? rows + row_offset(i, q, C) : H + (int64_t)(q + i * C) * ld;
+  };
   R* d = (R*)P.d;
   R* e = (R*)P.e;
   CX* tau = (CX*)P.tau;
@@ -82,14 +96,14 @@ __global__ void __launch_bounds__(512, 1) tridiag_cluster_kernel(const HeevdProb
   // ---- load own rows (lower triangle, scaled)
   for (int i = wid; i < nown; i += nw) {
     const int r = q + i * C;
-    CX* dst = rows + row_offset(i, q, C);
-    const CX* src = H + (int64_t)r * ld;
+    CX* dst = rowp(i);
+    const CX* src = H + (int64_t)r * ld;  // dst == src for an overflow row (scaled in place)
     for (int c = lane; c <= r; c += 32) dst[c] = cscale(src[c], inv);
   }
   __syncthreads();
   if (n == 1) {
     if (tid == 0) {
-      d[0] = rows[0].x;
+      d[0] = rowp(0)[0].x;
       e[0] = 0;
       tau[0] = czero<CX>();
     }
@@ -98,14 +112,14 @@ __global__ void __launch_bounds__(512, 1) tridiag_cluster_kernel(const HeevdProb
   bool prev_active = false;
   for (int j = 0; j <= n - 2; ++j) {
     // ---------------- A: publish column j (rows >= j+1) and the partial norm
-    if (q == (j % C) && tid == 0) d[j] = rows[row_offset(j / C, q, C) + j].x;
+    if (q == (j % C) && tid == 0) d[j] = rowp(j / C)[j].x;
     R part = 0;
     {
       // own rows r >= j+1: local index i >= i0
       const int i0 = (j + 1 - q + C - 1) / C > 0 ? (j + 1 - q + C - 1) / C : 0;
       for (int i = i0 + tid; i < nown; i += nt) {
         const int r = q + i * C;
-        const CX x = rows[row_offset(i, q, C) + j];
+        const CX x = rowp(i)[j];
         for (int k = 0; k < C; ++k) cluster.map_shared_rank(xbuf, k)[r] = x;
         if (r >= j + 2) part += cabs2(x);
       }
@@ -151,7 +165,7 @@ __global__ void __launch_bounds__(512, 1) tridiag_cluster_kernel(const HeevdProb
       const int i0 = (j + 1 - q + C - 1) / C > 0 ? (j + 1 - q + C - 1) / C : 0;
       for (int i = i0 + wid; i < nown; i += nw) {
         const int r = q + i * C;
-        CX* row = rows + row_offset(i, q, C);
+        CX* row = rowp(i);
         const CX vr = vprev[r], wr = wprev[r];
         CX acc = czero<CX>();
         for (int c = j + 1 + lane; c <= r; c += 32) {
@@ -178,7 +192,7 @@ __global__ void __launch_bounds__(512, 1) tridiag_cluster_kernel(const HeevdProb
           CX acc = czero<CX>();
           for (int i = (ic > i0 ? ic : i0); i < nown; ++i) {
             const int r = q + i * C;
-            cfma(acc, cconj(rows[row_offset(i, q, C) + c]), v[r]);
+            cfma(acc, cconj(rowp(i)[c]), v[r]);
           }
           pp[c] = cadd(pp[c], acc);
         }
@@ -205,7 +219,7 @@ __global__ void __launch_bounds__(512, 1) tridiag_cluster_kernel(const HeevdProb
       const int i0 = (j + 1 - q + C - 1) / C > 0 ? (j + 1 - q + C - 1) / C : 0;
       for (int i = i0 + tid; i < nown; i += nt) {
         const int r = q + i * C;
-        CX* a = rows + row_offset(i, q, C) + (j + 1);
+        CX* a = rowp(i) + (j + 1);
         CX val = *a;
         val = csub(val, cmul(v[r], cconj(wc)));
         val = csub(val, cmul(w[r], cconj(vc)));
@@ -221,7 +235,7 @@ __global__ void __launch_bounds__(512, 1) tridiag_cluster_kernel(const HeevdProb
     __syncthreads();
   }
   if (q == ((n - 1) % C) && tid == 0) {
-    d[n - 1] = rows[row_offset((n - 1) / C, q, C) + (n - 1)].x;
+    d[n - 1] = rowp((n - 1) / C)[n - 1].x;
     e[n - 1] = 0;
   }
   cluster.sync();  // keep every CTA's shared memory alive until remote readers finish
@@ -229,7 +243,7 @@ __global__ void __launch_bounds__(512, 1) tridiag_cluster_kernel(const HeevdProb
 
 }  // namespace
 
-// Shared memory bytes for cluster size C and matrix size n.
+// Shared memory bytes for cluster size C and matrix size n when every row fits.
 size_t tridiag_cluster_smem(int esz, int n, int C) {
   size_t best = 0;
   for (int q = 0; q < C && q < n; ++q) {
@@ -240,14 +254,51 @@ size_t tridiag_cluster_smem(int esz, int n, int C) {
   return (best + 6 * (size_t)n) * esz;
 }
 
-// Pick the cluster size (1..8 CTAs) for a matrix of size n.
+namespace {
+constexpr size_t kSmemBudget = 224 * 1024;
+
+// Largest cluster the device can co-schedule with `smem` bytes per CTA (16 needs
+// the non-portable opt-in); 0 if none.
+template <typename CX>
+int max_cluster(size_t smem) {
+  static int cached[2][2] = {{-1, -1}, {-1, -1}};
+  const int big = smem > 160 * 1024;
+  int& c = cached[sizeof(CX) == 16][big];
+  if (c >= 0) return c;
+  c = 8;
+  if (cudaFuncSetAttribute(tridiag_cluster_kernel<CX>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+      cudaSuccess) {
+    cudaFuncSetAttribute(tridiag_cluster_kernel<CX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBudget);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(16, 1, 1);
+    cfg.blockDim = dim3(512, 1, 1);
+    cfg.dynamicSmemBytes = kSmemBudget;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 16;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int nclusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&nclusters, tridiag_cluster_kernel<CX>, &cfg) == cudaSuccess && nclusters > 0)
+      c = 16;
+  }
+  cudaGetLastError();
+  return c;
+}
+}  // namespace
+
+// Pick the cluster size for a matrix of size n: the smallest of 1..8 CTAs whose
+// shared memory holds every row (at least 8 above n = 256, where the per-step
+// work, not the barriers, dominates); else the largest cluster the device
+// schedules, with the overflow rows in L2.
 int tridiag_cluster_size(int esz, int n) {
-  // The per-step work (not the barriers) dominates for n > 256, so large
-  // matrices take the largest portable cluster.
   const int lo = n > 256 ? 8 : 1;
   for (int C = lo; C <= 8; ++C)
-    if (tridiag_cluster_smem(esz, n, C) <= 224 * 1024) return C;
-  return 0;
+    if (tridiag_cluster_smem(esz, n, C) <= kSmemBudget) return C;
+  if (6 * (size_t)n * esz + 64 * 1024 > kSmemBudget) return 0;
+  return esz == 8 ? max_cluster<float2>(kSmemBudget) : max_cluster<double2>(kSmemBudget);
 }
 
 template <typename CX>
@@ -255,7 +306,10 @@ int launch_tridiag_cluster(const HeevdProb* probs, int count, int maxn, cudaStre
   const int esz = sizeof(CX);
   const int C = tridiag_cluster_size(esz, maxn);
   if (C == 0) return AGB_ERR_UNSUPPORTED;
-  const size_t smem = tridiag_cluster_smem(esz, maxn, C);
+  size_t smem = tridiag_cluster_smem(esz, maxn, C);
+  if (smem > kSmemBudget) smem = kSmemBudget;
+  const int cap_elems = (int)(smem / esz) - 6 * maxn;
+  if (C > 8) cudaFuncSetAttribute(tridiag_cluster_kernel<CX>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
   cudaFuncSetAttribute(tridiag_cluster_kernel<CX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(count * C, 1, 1);
@@ -269,7 +323,7 @@ int launch_tridiag_cluster(const HeevdProb* probs, int count, int maxn, cudaStre
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  cudaError_t err = cudaLaunchKernelEx(&cfg, tridiag_cluster_kernel<CX>, probs, C);
+  cudaError_t err = cudaLaunchKernelEx(&cfg, tridiag_cluster_kernel<CX>, probs, C, cap_elems);
   agb_note_launch();
   if (err != cudaSuccess) return AGB_ERR_CUDA;
   return AGB_OK;

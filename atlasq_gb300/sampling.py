@@ -15,7 +15,7 @@ from ._lib import check, dtype_code, ptr, stream_ptr
 
 
 def right_canonical_copy(mps):
-    ts = [t.to(mps.dtype).contiguous().clone() for t in mps._tensors]
+    ts = [t.to(mps.dtype).contiguous().clone() for t in mps.tensors]
     saved = list(mps._bond_dims)
     mps._right_sweep(ts)
     mps._bond_dims = saved

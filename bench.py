@@ -229,6 +229,138 @@ def reference_arm(args, dist, ws, rank):
     print(json.dumps(line), flush=True)
 
 
+def _timed(fn, device):
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    out = fn()
+    e.record()
+    e.synchronize()
+    return out, s.elapsed_time(e)
+
+
+def secondary_workload(args):
+    """One JSON line for a secondary workload (1 GPU):
+    batch256  256 HEA instances (n ~ U{16..48}, chi_max in {64,128,256}, 10 layers, eps 1e-8)
+              advanced together by MPSBatch; gates/s over all instances
+    sample50  50-qubit chi=256 Haar brickwork depth 16: 100,000 Philox shots, then 49 <Z_i Z_i+1>
+              and 50 <X_i>; shots/s (the state build is untimed)
+    hea64     64-qubit HEA, 12 layers of RY RZ + CZ ladder, chi_max 512, eps 1e-8; gates/s"""
+    import atlasq_gb300 as aq
+    from atlasq_gb300 import _lib
+    from atlasq_gb300.circuits import haar_brickwork, hea_circuit
+    lib = _lib.load()
+    device = torch.device("cuda", 0)
+    torch.cuda.set_device(device)
+    flush_buf = torch.empty(2 * L2_BYTES, dtype=torch.uint8, device=device)
+    line = {"n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "complex64", "data": "synthetic"}
+    if args.workload == "batch256":
+        rng = np.random.default_rng(2024)
+        specs = []
+        for b in range(256):
+            n = int(rng.integers(16, 49))
+            chi = int(rng.choice([64, 128, 256]))
+            ops = [(k, q, U.to(device)) for k, q, U in hea_circuit(n, 10, seed=50000 + b)]
+            specs.append((n, chi, ops))
+        ngates = sum(sum(1 for op in o if op[0] == "2q") for _, _, o in specs)
+
+        def one():
+            insts = [aq.AdaptiveMPS(n, bond_dim=1, eps_bond=1e-8, chi_max_per_bond=chi, device=device)
+                     for n, chi, _ in specs]
+            flush_buf.zero_()
+            (batch, ms) = _timed(lambda: aq.MPSBatch(insts).run([o for _, _, o in specs]), device)
+            return batch, insts, ms
+        for _ in range(args.warmup):
+            one()
+        launches0 = lib.agb_launch_count()
+        tot = 0.0
+        for _ in range(args.steps):
+            batch, insts, ms = one()
+            tot += ms
+        ms = tot / args.steps
+        line.update({"metric": "2-site gates/s, 256 HEA instances advanced together", "value": ngates / (ms / 1e3),
+                     "unit": "gates/s", "ms_per_step": ms,
+                     "gpu_launches": (lib.agb_launch_count() - launches0) // max(args.steps, 1),
+                     "config": {"workload": "256 HEA instances, n~U{16..48}, chi_max in {64,128,256}, 10 layers, eps 1e-8",
+                                "gates_per_step": ngates, "rounds_per_step": batch.rounds,
+                                "max_bond": max(max(m.bond_dims) for m in insts)}})
+    elif args.workload == "sample50":
+        from atlasq_gb300.sampling import right_canonical_copy, sample_tensors
+        ops = [(k, q, U.to(device)) for k, q, U in haar_brickwork(50, 16, seed=77)]
+        m = aq.AdaptiveMPS(50, bond_dim=1, eps_bond=1e-8, chi_max_per_bond=256, device=device)
+        for _, q, U in ops:
+            m.apply_two_site_gate(q, U)
+        m.flush()
+        Z = torch.tensor([[1, 0], [0, -1]], dtype=torch.complex64)
+        X = torch.tensor([[0, 1], [1, 0]], dtype=torch.complex64)
+        obs = [{i: Z, i + 1: Z} for i in range(49)] + [{i: X} for i in range(50)]
+        shots = 100000
+
+        def one():
+            flush_buf.zero_()
+            def work():
+                ts = right_canonical_copy(m)
+                bits = sample_tensors(ts, shots, seed=5)
+                vals = aq.local_expectations(m, obs)
+                return bits, vals
+            return _timed(work, device)
+        for _ in range(args.warmup):
+            one()
+        launches0 = lib.agb_launch_count()
+        tot = 0.0
+        for _ in range(args.steps):
+            (bits, vals), ms = one()
+            tot += ms
+        ms = tot / args.steps
+        launches = (lib.agb_launch_count() - launches0) // max(args.steps, 1)
+        # sampling alone
+        ts = right_canonical_copy(m)
+        torch.cuda.synchronize()
+        _, ms_s = _timed(lambda: sample_tensors(ts, shots, seed=5), device)
+        _, ms_e = _timed(lambda: aq.local_expectations(m, obs), device)
+        chis = [t.shape[0] for t in ts] + [1]
+        flops = sum(8.0 * 2 * shots * chis[i] * chis[i + 1] for i in range(50))  # complex MACs: L[ns,l] x T[l,2r]
+        line.update({"metric": "shots/s (100k Philox shots + 99 local expectations, 50q chi=256)",
+                     "value": shots / (ms / 1e3), "unit": "shots/s", "ms_per_step": ms, "gpu_launches": launches,
+                     "config": {"workload": "50-qubit Haar brickwork depth 16, chi_max 256; 100,000 shots; 49 ZZ + 50 X",
+                                "max_bond": max(chis)},
+                     "parts_ms": {"right_canonicalise+sample": ms_s, "expectations": ms_e},
+                     "sampling_tflops": flops / (ms_s / 1e3) / 1e12,
+                     "zz0": vals[0].real, "x0": vals[49].real})
+    else:
+        ops = [(k, q, U.to(device)) for k, q, U in hea_circuit(64, 12, seed=64)]
+        ngates = sum(1 for op in ops if op[0] == "2q")
+
+        def one():
+            m = aq.AdaptiveMPS(64, bond_dim=1, eps_bond=1e-8, chi_max_per_bond=512, device=device)
+            flush_buf.zero_()
+
+            def work():
+                for k, q, U in ops:
+                    (m.apply_two_site_gate if k == "2q" else m.apply_single_qubit_gate)(q, U)
+                m.flush()
+                return m
+            return _timed(work, device)
+        for _ in range(args.warmup):
+            one()
+        lib.agb_prof_begin(200000)
+        tot = 0.0
+        for _ in range(args.steps):
+            m, ms = one()
+            tot += ms
+        ms = tot / args.steps
+        ms_st = (ctypes.c_double * 16)()
+        cnt_st = (ctypes.c_int * 16)()
+        _lib.check(lib.agb_prof_end(ms_st, cnt_st, 16), "prof_end")
+        line.update({"metric": "2-site gates/s, 64q HEA 12 layers chi=512", "value": ngates / (ms / 1e3),
+                     "unit": "gates/s", "ms_per_step": ms,
+                     "config": {"workload": "64-qubit HEA, 12 layers RY RZ + CZ ladder, chi_max 512, eps 1e-8",
+                                "gates_per_step": ngates, "max_bond": max(m.bond_dims)},
+                     "stage_ms_per_step": {nm: round(ms_st[i] / args.steps, 3) for i, nm in enumerate(_lib.STAGES)}})
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -238,7 +370,12 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--fp64-check", action="store_true", help="also run the complex128 GPU path and report fidelity")
+    ap.add_argument("--workload", default="brickwork40", choices=["brickwork40", "batch256", "sample50", "hea64"],
+                    help="brickwork40 is the headline; the others are the secondary workloads")
     args = ap.parse_args()
+    if args.workload != "brickwork40" and args.impl == "ours":
+        secondary_workload(args)
+        return
 
     dist, ws, rank, local = dist_init()
     if args.impl == "reference":

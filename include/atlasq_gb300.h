@@ -103,6 +103,14 @@ int agb_two_site_finalize(int dtype, int ngates, const int64_t* desc_dev, int ma
  * (U^T; src/atlas_q/adaptive_mps.py:159-180).  In place. */
 int agb_single_qubit_gate(int dtype, void* T, const void* U, int chiL, int chiR, void* stream);
 
+/* Queued single-qubit gates of many sites (and many MPS instances) in one launch,
+ * same arithmetic per gate as agb_single_qubit_gate.  desc (device, int64):
+ * [ngroups][5] = {T, chiL, chiR, first, count} followed by the gate pointers
+ * (2x2 matrices of the tensor's type); group g applies gates first..first+count-1
+ * to T in order.  Groups must name distinct tensors.  max_elems >= chiL*chiR of
+ * every group.  ngroups <= 65535. */
+int agb_single_qubit_batch(int dtype, int ngroups, const int64_t* desc, int max_elems, void* stream);
+
 /* Hermitian eigensolver (batched), exposed for robust_svd / tests.
  * Replaces the torch.linalg.svd call inside robust_svd (linalg_robust.py:37) when
  * used as X -> Gram -> eigenpairs.  H: [batch, n, n] Hermitian (overwritten);
@@ -160,6 +168,22 @@ int agb_prof_begin(int capacity);
 /* Number of kernels this library has launched since it was loaded. */
 long long agb_launch_count(void);
 int agb_prof_end(double* ms_per_stage, int* marks_per_stage, int nstages);
+
+/* (a14) Learned rank predictor: MLP 5 -> 64 -> 64 -> 64 -> 1 (ReLU hidden,
+ * sigmoid output), FP32, parameters in one buffer of AGB_MLP_NPARAM floats
+ * (W1[64][5] b1 W2[64][64] b2 W3[64][64] b3 W4[64] b4).  New in this build:
+ * the reference's predictor (src/atlas_q/tools_qih/ai_rank_predictor.py:14-89)
+ * reads singular values after the SVD; this one predicts the kept rank before
+ * it from (chi_L, chi_R, entangling power, neighbouring-bond entropy, previous
+ * rank).  X: [B][5] features, Y/T: [B] rank fraction in (0, 1).
+ * agb_mlp_backward zeroes `grads` and accumulates d mean((y-t)^2) / d params;
+ * loss_sum (optional) receives sum (y-t)^2.  agb_mlp_adam is AdamW (step >= 1). */
+#define AGB_MLP_NPARAM 8769
+int agb_mlp_forward(const float* params, const float* X, int B, float* Y, void* stream);
+int agb_mlp_backward(const float* params, const float* X, const float* T, int B, float* grads, float* loss_sum,
+                     void* stream);
+int agb_mlp_adam(float* params, const float* grads, float* m, float* v, int step, float lr, float beta1,
+                 float beta2, float eps, float weight_decay, void* stream);
 
 /* Batched complex64 GEMM on the tcgen05 tensor cores (3xTF32 split precision,
  * TMA-fed), strided batch: C[b] = alpha op(A[b]) op(B[b]) + beta C[b].

@@ -5,6 +5,7 @@ reference's golden vectors.  Tolerances are written in each test:
   * two-site update vs reference: kept singular values within 1e-5 * sigma_0,
     identical bond dimensions, state fidelity >= 1 - 1e-6.
 """
+import functools
 import numpy as np
 import pytest
 import torch
@@ -80,10 +81,11 @@ def test_cgemm_tensor_cores_3xtf32(opA, opB, M, N, K, batch):
     assert rel(C, ref) < 1e-6 + 2e-9 * K
 
 
+@functools.lru_cache(maxsize=1)
 def _hermitian_cases():
     g = torch.Generator().manual_seed(11)
     cases = []
-    for n in (1, 2, 5, 33, 128, 300, 512):
+    for n in (1, 2, 5, 33, 128, 300, 512, 800, 1024):
         X = crandn(n + 3, n, gen=g, dtype=torch.complex128)
         cases.append(("gram", X.conj().T @ X))
     # rank deficient Gram (rank 40 of 96)
@@ -108,9 +110,11 @@ def _hermitian_cases():
     return cases
 
 
-@pytest.mark.parametrize("case", range(12))
+@pytest.mark.parametrize("case", range(14))
 @pytest.mark.parametrize("dt", [torch.complex64, torch.complex128])
 def test_heevd_residual_and_orthonormality(case, dt):
+    """Sizes 800 and 1024 (and 512 in complex128) exercise the cluster
+    tridiagonalisation with rows overflowing shared memory into L2."""
     name, H = _hermitian_cases()[case]
     H = (H + H.conj().T) / 2
     n = H.shape[0]
@@ -414,3 +418,36 @@ def test_amplitudes_and_robust_svd():
     assert np.max(np.abs(S.cpu().numpy() - ref)) < 1e-5 * ref[0]
     assert rel(((U * S.to(U.dtype)) @ Vh).cpu().numpy(), X.cpu().numpy()) < 1e-5
     assert drv == "gb300_gram_heevd"
+
+
+@pytest.mark.parametrize("chiM,eps", [(512, 1e-8), (96, 1e-8), (512, 1e-2)])
+def test_two_site_chi512_matches_svd(chiM, eps):
+    """chi_L = chi_R = 512 (X is 1024 x 1024, the chi_max=512 workload): kept rank,
+    discarded weight and the truncated two-site block match a float64 SVD of the
+    same X; chiM = 96 makes X rank-deficient (384 of 1024)."""
+    gen = torch.Generator().manual_seed(chiM)
+    A = crandn(512, 2, chiM, gen=gen, dtype=torch.complex128)
+    B = crandn(chiM, 2, 512, gen=gen, dtype=torch.complex128)
+    decay = torch.exp(-torch.arange(chiM, dtype=torch.float64) / 60.0)  # graded spectrum
+    A = A * decay[None, None, :]
+    A, B = A / A.norm(), B / B.norm()
+    U = haar_unitary(gen).to(torch.complex128)
+    m = aq.AdaptiveMPS(2, bond_dim=1, eps_bond=eps, chi_max_per_bond=512, device=DEV)
+    m._tensors = [A.to(torch.complex64).to(DEV), B.to(torch.complex64).to(DEV)]
+    m._bond_dims = [chiM]
+    m.apply_two_site_gate(0, U.to(torch.complex64))
+    m.flush()
+    A32, B32 = A.to(torch.complex64).numpy(), B.to(torch.complex64).numpy()
+    X = mo.fused_two_qubit_gate(A32.astype(np.complex128), B32.astype(np.complex128),
+                                U.to(torch.complex64).numpy().astype(np.complex128))
+    Uu, S, Vh = np.linalg.svd(X, full_matrices=False)
+    k_ref = mo.choose_rank_from_sigma(S.astype(np.float32), eps, 512)[0]
+    k = m.bond_dims[0]
+    assert abs(k - k_ref) <= 1, (k, k_ref)
+    Xt = (Uu[:, :k] * S[:k]) @ Vh[:k]
+    Y = (m.tensors[0].cpu().numpy().reshape(1024, k).astype(np.complex128) @
+         m.tensors[1].cpu().numpy().reshape(k, 1024).astype(np.complex128))
+    f = abs(np.vdot(Xt, Y)) ** 2 / (np.vdot(Xt, Xt).real * np.vdot(Y, Y).real)
+    assert f > 1 - 1e-6, f
+    disc = np.sqrt(max(0.0, (S ** 2).sum() - (S[:k] ** 2).sum()))
+    assert abs(m.statistics.logs["eps_local"][0] - disc) <= 1e-5 * S[0] + 1e-3 * disc
