@@ -28,6 +28,7 @@ AGB_C128 = 1
 D_A, D_B, D_U, D_CHIL, D_CHIM, D_CHIR, D_CAP, D_EPS = 0, 1, 2, 3, 4, 5, 6, 7
 D_ANEW, D_BNEW, D_ELL, D_SEED, D_WS = 8, 9, 10, 11, 12
 D_K, D_EPSLOC, D_ENTROPY, D_CONDS, D_STATUS, D_TOTAL, D_NEEDED, D_MODE = 16, 17, 18, 19, 20, 21, 22, 23
+D_DIMS, D_BOND, D_CAPL, D_CAPM, D_CAPR, D_ELLPLAN, D_NVEC = 24, 25, 26, 27, 28, 29, 30
 D_NFIELDS = 32
 
 MLP_NPARAM = 8769

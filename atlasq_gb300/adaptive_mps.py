@@ -24,7 +24,7 @@ from typing import Dict, List, Optional, Union
 import numpy as np
 import torch
 
-from . import _lib, ops
+from . import _lib, ops, resident
 from ._lib import check, dtype_code, ptr, stream_ptr
 from .diagnostics import MPSStatistics
 from .truncation import check_entropy_sanity
@@ -54,7 +54,8 @@ class AdaptiveMPS:
     def __init__(self, num_qubits: int, bond_dim: int = 8, *, eps_bond: float = 1e-6,
                  chi_max_per_bond: Optional[Union[int, List[int]]] = 256,
                  budget_global_mb: Optional[float] = None, dtype_policy: DTypePolicy = DTypePolicy(),
-                 device: str = "cuda", dtype: Optional[torch.dtype] = None, seed: int = 0):
+                 device: str = "cuda", dtype: Optional[torch.dtype] = None, seed: int = 0,
+                 device_resident: bool = False):
         if dtype is None:
             dtype = dtype_policy.default
         self.device = _lib.require_cuda(device)
@@ -82,6 +83,10 @@ class AdaptiveMPS:
         self.feature_log = None      # list -> (features, k, full) per gate is appended (predictor training data)
         self._last_entropy = {}      # bond -> entanglement entropy at its last update
         self.rank_fallbacks = 0      # gates re-run at full size after a too-small predicted ell
+        # device-resident mode (see resident.py): gates run without host synchronisation
+        self.device_resident = device_resident
+        self._res = None
+        self.unpromoted = 0
         self.ell_total = 0           # eigenpairs computed, summed over gates (fallback runs included)
         self.batch_log = []          # per-flush (n_gates, seconds) for profiling
         self._initialize_zero_state(bond_dim)
@@ -116,16 +121,35 @@ class AdaptiveMPS:
         self._tensors = tensors
         self.is_canonical = True
 
-    def _flush(self):
+    def _drain(self):
+        """Apply the queued gates (staying in resident mode if active)."""
         if self._pending_1q:
             g1 = self._pending_1q
             self._pending_1q = []
-            apply_single_qubit_entries([(self, q, U) for q, U in g1])
+            if self._res is not None:
+                resident.single_qubit_entries([(self, q, U) for q, U in g1])
+            else:
+                apply_single_qubit_entries([(self, q, U) for q, U in g1])
         if self._pending:
             gates = self._pending
             self._pending = []
             self._pending_sites = set()
-            self._apply_batch(gates)
+            if self._res is not None:
+                resident.two_site_entries([(self, i, U) for i, U in gates])
+            else:
+                self._apply_batch(gates)
+
+    def _flush(self):
+        """Apply the queued gates and return to host-visible tensors."""
+        self._drain()
+        if self._res is not None:
+            resident.leave(self)
+
+    def _maybe_enter_resident(self):
+        if (self.device_resident and self._res is None and self.rank_predictor is None
+                and self.budget_global_mb is None and self.feature_log is None):
+            self._drain()
+            resident.enter(self)
 
     def flush(self):
         """Apply all queued two-site gates now."""
@@ -180,8 +204,9 @@ class AdaptiveMPS:
         two-site gate flushes first, so the order of operations is kept)."""
         assert 0 <= q < self.num_qubits, f"Qubit index {q} out of range"
         assert U2.shape == (2, 2), "U2 must be 2x2"
+        self._maybe_enter_resident()
         if q in self._pending_sites:
-            self._flush()
+            self._drain()
         self._pending_1q.append((q, U2))
         self.is_canonical = False
 
@@ -195,8 +220,9 @@ class AdaptiveMPS:
             U = U4
         else:
             raise ValueError(f"U4 must be (2,2,2,2) or (4,4), got {U4.shape}")
+        self._maybe_enter_resident()
         if i in self._pending_sites or (i + 1) in self._pending_sites:
-            self._flush()
+            self._drain()
         self._pending.append((i, U))
         self._pending_sites.update((i, i + 1))
         self.is_canonical = False
@@ -524,7 +550,7 @@ def apply_gate_entries(entries):
     # rank fallback: predicted size too small -> rerun those gates at full size
     redo = [g for g, r in enumerate(res) if r["status"] == _lib.AGB_ERR_RANK]
     if redo:
-        full = _run_pipeline([entries[g] for g in redo], dt, None)
+        full = _run_pipeline([entries[g] for g in redo], dt, None, all_vectors=True)
         for g, r in zip(redo, full):
             r["driver"] = "gb300_gram_heevd_full"
             res[g] = r
@@ -535,7 +561,7 @@ def apply_gate_entries(entries):
                if math.isfinite(r["condS"]) and r["condS"] > entries[g][0].dtype_policy.promote_if_cond_gt
                and dt != _C128]
     if promote:
-        r2 = _run_pipeline([entries[g] for g in promote], _C128, None)
+        r2 = _run_pipeline([entries[g] for g in promote], _C128, None, all_vectors=True)
         for g, r in zip(promote, r2):
             r["driver"] = "gb300_gram_heevd_c128"
             res[g] = r
@@ -559,8 +585,11 @@ def apply_gate_entries(entries):
                              dtype=str(r["dtype"]), ms_elapsed=elapsed, condS=r["condS"])
 
 
-def _run_pipeline(entries, dt, ells):
+def _run_pipeline(entries, dt, ells, all_vectors=False):
     """One batched launch sequence: plan -> run -> read ranks -> finalize.
+    By default the device computes eigenvectors only for the eigenvalues the
+    rank rule can keep (AGB_D_NVEC = 0); ``all_vectors`` computes every one
+    (the re-run of a gate that reported AGB_ERR_RANK).
     Descriptor rows are built and read with NumPy; the two small copies per
     batch (descriptors up, results down) are the only host synchronisation."""
     lib = _lib.load()
@@ -604,6 +633,7 @@ def _run_pipeline(entries, dt, ells):
         row[_lib.D_EPS] = _dbits(m.eps_bond)
         row[_lib.D_ELL] = int(ells[g]) if ells is not None else 0
         row[_lib.D_SEED] = seed
+        row[_lib.D_NVEC] = -1 if all_vectors else 0
         meta.append((m, i, chiL, chiM, chiR))
     wsz = _lib.SZ(0)
     check(lib.agb_two_site_plan(code, G, desc.ctypes.data_as(ctypes.c_void_p), ctypes.byref(wsz)),

@@ -34,7 +34,11 @@ __global__ void __launch_bounds__(256) single_qubit_batch_kernel(const int64_t* 
   __shared__ CX su[SQ_CHUNK * 4];
   const int64_t* G = desc + (int64_t)blockIdx.y * 5;
   CX* T = (CX*)G[0];
-  const int chiL = (int)G[1], chiR = (int)G[2];
+  // chiL < 0: device-resident tensor; G[2] then points at its two bond
+  // dimensions (left, right) in the instance's int32 dimension array
+  const bool res = G[1] < 0;
+  const int chiL = res ? ((const int*)G[2])[0] : (int)G[1];
+  const int chiR = res ? ((const int*)G[2])[1] : (int)G[2];
   const int64_t first = G[3];
   const int cnt = (int)G[4];
   const int64_t* up = desc + (int64_t)ngroups * 5 + first;

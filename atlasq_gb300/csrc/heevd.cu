@@ -260,8 +260,8 @@ template <typename R> AGB_DEV bool in_cluster(const R* lam, int ell, int t, R to
 template <typename R>
 __global__ void __launch_bounds__(128) invit_kernel(const HeevdProb* __restrict__ probs) {
   const HeevdProb P = probs[blockIdx.y];
-  const int n = P.n, ell = P.ell;
-  if (blockIdx.x * 128 >= ell) return;
+  const int n = P.n, ell = P.ell, nv = P.nvec;
+  if (blockIdx.x * 128 >= nv) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   R* d = (R*)smem_raw;
   R* e = d + n;
@@ -271,8 +271,8 @@ __global__ void __launch_bounds__(128) invit_kernel(const HeevdProb* __restrict_
   }
   __syncthreads();
   const int t = blockIdx.x * 128 + threadIdx.x;
-  if (t >= ell || P.skip_vectors) return;
-  if (in_cluster((const R*)P.lam, ell, t, cluster_tol((const R*)P.lam, ell, 1e-5))) return;
+  if (t >= nv || P.skip_vectors) return;
+  if (in_cluster((const R*)P.lam, nv, t, cluster_tol((const R*)P.lam, ell, kClusterTolRel))) return;
   const R lam = ((const R*)P.lam)[t];
   R tnorm = 0;
   for (int i = 0; i < n; ++i) tnorm = fmax(tnorm, fabs(d[i]) + fabs(e[i]) + (i ? fabs(e[i - 1]) : R(0)));
@@ -483,47 +483,67 @@ AGB_DEV R tri_solve(R* Y, int n, const R* U0, const R* U1, const R* U2, const R*
   return nrm;
 }
 
-// CGS2 of column j against columns [t0, j) and normalisation (block-wide).
+// CGS2 of the working column y (shared memory) against columns [t0, j) of Y
+// and normalisation (block-wide).  Dot products: tiles of 32 columns, lanes
+// over the columns (coalesced rows of Y), warps over row groups, partial sums
+// combined in shared memory; update: one warp per row, lanes over the columns.
 template <typename R>
-AGB_DEV void cgs2_normalize(R* Y, int n, int64_t L, int t0, int j, R* coef, R* red) {
-  const int tid = threadIdx.x, nt = blockDim.x;
-  for (int pass = 0; pass < 2; ++pass) {
-    if (j > t0) {
-      for (int i = t0 + tid; i < j; i += nt) {
-        R acc = 0;
-        for (int r = 0; r < n; ++r) acc += Y[r * L + i] * Y[r * L + j];
-        coef[i - t0] = acc;
+AGB_DEV void cgs2_normalize(R* y, const R* Y, int n, int64_t L, int t0, int j, R* coef, R* red, R* part) {
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, wid = tid >> 5, nw = nt >> 5;
+  const int cols = j - t0;
+  for (int pass = 0; pass < 2 && cols > 0; ++pass) {
+    for (int c0 = 0; c0 < cols; c0 += 32) {
+      const int c = c0 + lane;
+      R a0 = 0, a1 = 0;
+      if (c < cols) {
+        const R* col = Y + t0 + c;
+        int r = wid;
+        for (; r + nw < n; r += 2 * nw) {
+          a0 += col[(int64_t)r * L] * y[r];
+          a1 += col[(int64_t)(r + nw) * L] * y[r + nw];
+        }
+        if (r < n) a0 += col[(int64_t)r * L] * y[r];
       }
+      part[wid * 32 + lane] = a0 + a1;
       __syncthreads();
-      for (int r = tid; r < n; r += nt) {
-        R acc = 0;
-        for (int i = t0; i < j; ++i) acc += coef[i - t0] * Y[r * L + i];
-        Y[r * L + j] -= acc;
+      if (wid == 0 && c < cols) {
+        R sum = 0;
+        for (int w = 0; w < nw; ++w) sum += part[w * 32 + lane];
+        coef[c] = sum;
       }
       __syncthreads();
     }
+    for (int r = wid; r < n; r += nw) {
+      const R* row = Y + (int64_t)r * L + t0;
+      R acc = 0;
+      for (int c = lane; c < cols; c += 32) acc += coef[c] * row[c];
+      acc = warp_sum(acc);
+      if (lane == 0) y[r] -= acc;
+    }
+    __syncthreads();
   }
-  R part = 0;
-  for (int r = tid; r < n; r += nt) part += Y[r * L + j] * Y[r * L + j];
-  const R nrm = block_sum(part, red);
+  R psum = 0;
+  for (int r = tid; r < n; r += nt) psum += y[r] * y[r];
+  const R nrm = block_sum(psum, red);
   const R sc = R(1) / sqrt(fmax(nrm, rlim<R>::pivmin()));
-  for (int r = tid; r < n; r += nt) Y[r * L + j] *= sc;
+  for (int r = tid; r < n; r += nt) y[r] *= sc;
   __syncthreads();
 }
 
 template <typename R>
 __global__ void __launch_bounds__(256) cluster_invit_kernel(const HeevdProb* __restrict__ probs, double tolrel) {
   const HeevdProb P = probs[blockIdx.y];
-  const int n = P.n, ell = P.ell;
-  if (ell < 2 || P.skip_vectors) return;
+  const int n = P.n, ell = P.ell, nv = P.nvec;
+  if (nv < 2 || P.skip_vectors) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   R* d = (R*)smem_raw;   // [n]
   R* e = d + n;          // [n]
   R* coef = e + n;       // [ell]
   R* f = coef + ell;     // [5n] LU factors of the current member (U0,U1,U2,L,P)
-  R* ycol = f + 5 * n;   // [n]  working column for the serial solve
+  R* ycol = f + 5 * n;   // [n]  working column of the current member
   __shared__ int cl_t0, cl_t1;
   __shared__ R red[32];
+  __shared__ R part[256];
   __shared__ R s_shift, s_nrm;
   const R* lamg = (const R*)P.lam;
   const int tid = threadIdx.x, nt = blockDim.x;
@@ -533,8 +553,8 @@ __global__ void __launch_bounds__(256) cluster_invit_kernel(const HeevdProb* __r
   if (tid == 0) {
     const R tol = cluster_tol(lam, ell, tolrel);
     int found = -1, s = 0, t0 = -1, t1 = -1;
-    for (int t = 1; t <= ell; ++t) {
-      if (t == ell || (lam[t - 1] - lam[t]) > tol) {
+    for (int t = 1; t <= nv; ++t) {
+      if (t == nv || (lam[t - 1] - lam[t]) > tol) {
         if (t - s > 1) {
           ++found;
           if (found == (int)blockIdx.x) {
@@ -559,18 +579,18 @@ __global__ void __launch_bounds__(256) cluster_invit_kernel(const HeevdProb* __r
   }
   __syncthreads();
   R tnorm = 0;
-  for (int i = 0; i < n; ++i) tnorm = fmax(tnorm, fabs(d[i]) + fabs(e[i]) + (i ? fabs(e[i - 1]) : R(0)));
+  for (int i = tid; i < n; i += nt) tnorm = fmax(tnorm, fabs(d[i]) + fabs(e[i]) + (i ? fabs(e[i - 1]) : R(0)));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) tnorm = fmax(tnorm, __shfl_xor_sync(0xffffffffu, tnorm, o));
+  if ((tid & 31) == 0) red[tid >> 5] = tnorm;
+  __syncthreads();
+  tnorm = 0;
+  for (int w = 0; w < (nt >> 5); ++w) tnorm = fmax(tnorm, red[w]);
+  __syncthreads();
   const R piv = rlim<R>::eps() * fmax(tnorm, rlim<R>::pivmin());
   const R pert = R(10) * rlim<R>::eps() * fmax(tnorm, rlim<R>::pivmin());
-  R* lu = (R*)P.lu;
   const int64_t L = ell;
-  R* U0 = lu;
-  R* U1 = lu + (int64_t)n * L;
-  R* U2 = lu + 2 * (int64_t)n * L;
-  R* Lm = lu + 3 * (int64_t)n * L;
-  R* Pv = lu + 4 * (int64_t)n * L;
   R* Y = (R*)P.Y;
-  (void)U0; (void)U1; (void)U2; (void)Lm; (void)Pv;
   R prev = 0;
   for (int j = t0; j < t1; ++j) {
     if (tid == 0) {
@@ -579,24 +599,22 @@ __global__ void __launch_bounds__(256) cluster_invit_kernel(const HeevdProb* __r
       s_shift = sh;
       tri_lu(d, e, n, sh, piv, f, f + n, f + 2 * n, f + 3 * n, f + 4 * n, 1, 0);
     }
-    for (int r = tid; r < n; r += nt) Y[r * L + j] = (R)philox_normal(P.seed, (uint64_t)j * (uint64_t)n + r, 0x11u);
+    for (int r = tid; r < n; r += nt) ycol[r] = (R)philox_normal(P.seed, (uint64_t)j * (uint64_t)n + r, 0x11u);
     __syncthreads();
     prev = s_shift;
     for (int it = 0; it < 2; ++it) {
-      cgs2_normalize(Y, n, L, t0, j, coef, red);
-      for (int r = tid; r < n; r += nt) ycol[r] = Y[r * L + j];
-      __syncthreads();
+      cgs2_normalize(ycol, Y, n, L, t0, j, coef, red, part);
       if (tid == 0) s_nrm = tri_solve(ycol, n, f, f + n, f + 2 * n, f + 3 * n, f + 4 * n, 1, 0, piv);
-      __syncthreads();
-      for (int r = tid; r < n; r += nt) Y[r * L + j] = ycol[r];
       __syncthreads();
       if (!(s_nrm < R(1e300)) || !(s_nrm > R(0))) {
         for (int r = tid; r < n; r += nt)
-          Y[r * L + j] = (R)philox_normal(P.seed ^ 0xABCDEFull, (uint64_t)(j + it + 1) * (uint64_t)n + r, 0x13u);
+          ycol[r] = (R)philox_normal(P.seed ^ 0xABCDEFull, (uint64_t)(j + it + 1) * (uint64_t)n + r, 0x13u);
         __syncthreads();
       }
     }
-    cgs2_normalize(Y, n, L, t0, j, coef, red);
+    cgs2_normalize(ycol, Y, n, L, t0, j, coef, red, part);
+    for (int r = tid; r < n; r += nt) Y[(int64_t)r * L + j] = ycol[r];
+    __syncthreads();
   }
 }
 
@@ -616,7 +634,7 @@ __global__ void polish_setup_kernel(const HeevdProb* __restrict__ probs, GemmPro
   GemmProb g;
   g.A = Vs; g.B = Vs; g.D = P.M; g.Csrc = P.M;
   g.lda = lds; g.ldb = lds; g.ldd = P.ell; g.ldc = P.ell;
-  g.M = P.ell; g.N = P.ell; g.K = P.n;
+  g.M = P.nvec; g.N = P.nvec; g.K = P.n;
   g.opA = 2; g.opB = 0;
   g.alpha_re = 1; g.alpha_im = 0; g.beta_re = 0; g.beta_im = 0;
   if (P.skip_vectors) g.M = 0;
@@ -624,7 +642,7 @@ __global__ void polish_setup_kernel(const HeevdProb* __restrict__ probs, GemmPro
   GemmProb h;
   h.A = Vs; h.B = P.M; h.D = Vd; h.Csrc = Vs;
   h.lda = lds; h.ldb = P.ell; h.ldd = ldd; h.ldc = lds;
-  h.M = P.n; h.N = P.ell; h.K = P.ell;
+  h.M = P.n; h.N = P.nvec; h.K = P.nvec;
   h.opA = 0; h.opB = 0;
   h.alpha_re = -0.5; h.alpha_im = 0; h.beta_re = 1.5; h.beta_im = 0;
   if (P.skip_vectors) h.M = 0;
@@ -638,13 +656,13 @@ template <typename CX, int NK, int WARPS>
 __global__ void __launch_bounds__(WARPS * 32) backtransform2_kernel(const HeevdProb* __restrict__ probs) {
   typedef typename cx_traits<CX>::R R;
   const HeevdProb P = probs[blockIdx.y];
-  const int n = P.n, ell = P.ell;
+  const int n = P.n, ell = P.ell, nv = P.nvec;
   const int col0 = blockIdx.x * 2 * WARPS;
-  if (col0 >= ell || n > NK * 32 || P.skip_vectors) return;
+  if (col0 >= nv || n > NK * 32 || P.skip_vectors) return;
   __shared__ CX vbuf[2][NK * 32];
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const int t0 = col0 + 2 * wid, t1 = t0 + 1;
-  const bool h0 = t0 < ell, h1 = t1 < ell;
+  const bool h0 = t0 < nv, h1 = t1 < nv;
   const R* Y = (const R*)P.Y;
   CX z0[NK], z1[NK];
 #pragma unroll
@@ -752,7 +770,7 @@ int launch_heevd_vectors(HeevdProb* probs, GemmProb* gp, int count, int maxn, in
     if (sm > 48 * 1024)
       cudaFuncSetAttribute(cluster_invit_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     const int maxcl = maxell / 2 > 0 ? maxell / 2 : 1;
-    cluster_invit_kernel<R><<<dim3(maxcl, count), 256, sm, s>>>(probs, 1e-5);
+    cluster_invit_kernel<R><<<dim3(maxcl, count), 256, sm, s>>>(probs, kClusterTolRel);
     AGB_CHECK_LAUNCH();
   }
   int rc;
@@ -802,6 +820,7 @@ __global__ void heevd_setup_kernel(HeevdProb* probs, void* H, void* evecs, char*
   p.ldv = ell;
   p.seed = seed + 0x9E3779B97F4A7C15ull * (uint64_t)b;
   p.skip_vectors = 0;
+  p.nvec = ell;
   heevd_assign_scratch_dev(p, scratch + (size_t)b * scratch_stride, esz);
   probs[b] = p;
 }

@@ -16,6 +16,12 @@
 #pragma once
 #include "gemm.cuh"
 
+// Eigenvalues closer than kClusterTolRel * max|lambda| are solved as a cluster
+// (re-orthogonalised inverse iteration).  Wider gaps leave inverse-iteration
+// vectors at most ~eps*||T||/gap (< 0.1 in float32) from orthogonal, which the
+// Newton-Schulz polish removes.
+constexpr double kClusterTolRel = 1e-6;
+
 struct HeevdProb {
   void* H;       // CX[n x ldh], Hermitian input, overwritten by the reduction
   int64_t ldh;
@@ -33,6 +39,8 @@ struct HeevdProb {
   void* scale;   // R[1] scale applied to H (eigenvalues of H = lam * scale)
   uint64_t seed;
   int skip_vectors;  // set by the caller between the two phases: no eigenvectors needed
+  int nvec;          // eigenvectors to compute (the leading nvec of the ell eigenvalues), <= ell;
+                     // may be lowered between the two phases; strides stay ell
 };
 
 // Bytes of per-problem scratch (d, e, tau, lam, Y, lu, V2, M, scale) for one

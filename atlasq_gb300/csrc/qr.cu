@@ -17,7 +17,7 @@ constexpr int QR_CG = 128, QR_RG = 8;
 
 template <typename CX>
 __global__ void __launch_bounds__(1024) qr_kernel(const CX* __restrict__ Ain, int M, int N, int transA,
-                                                  CX* W, CX* Q, CX* R, int trans_out, CX* tau) {
+                                                  CX* W, CX* Q, CX* R, int trans_out, CX* tau, CX* Qw) {
   typedef typename cx_traits<CX>::R Rt;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   CX* v = (CX*)smem_raw;                 // [M]
@@ -94,11 +94,13 @@ __global__ void __launch_bounds__(1024) qr_kernel(const CX* __restrict__ Ain, in
   }
   // Q = H_0 ... H_{kk-1} [I; 0]: apply the reflectors (stored below the diagonal
   // of W, unit leading entry) in reverse order to the first kk identity columns.
-  // Element (r, c) of Q lives at r*kk + c, or at c*M + r when transposed.
-  const int64_t qs_r = trans_out ? 1 : kk, qs_c = trans_out ? M : 1;
+  // Q is formed row-major (element (r, c) at r*kk + c, column lanes coalesced);
+  // a transposed output is formed in the workspace and copied out at the end.
+  CX* Qf = trans_out ? Qw : Q;
+  const int64_t qs_r = kk, qs_c = 1;
   for (int64_t i = tid; i < (int64_t)M * kk; i += nt) {
     const int r = (int)(i / kk), c = (int)(i % kk);
-    Q[r * qs_r + c * qs_c] = (r == c) ? mk<CX>(1, 0) : czero<CX>();
+    Qf[r * qs_r + c * qs_c] = (r == c) ? mk<CX>(1, 0) : czero<CX>();
   }
   __syncthreads();
   for (int j = kk - 1; j >= 0; --j) {
@@ -110,7 +112,7 @@ __global__ void __launch_bounds__(1024) qr_kernel(const CX* __restrict__ Ain, in
       const int c = c0 + cg;
       CX acc = czero<CX>();
       if (c < kk)
-        for (int r = j + rg; r < M; r += QR_RG) cfmac(acc, v[r], Q[r * qs_r + c * qs_c]);
+        for (int r = j + rg; r < M; r += QR_RG) cfmac(acc, v[r], Qf[r * qs_r + c * qs_c]);
       part[rg * QR_CG + cg] = acc;
       __syncthreads();
       if (c < kk) {
@@ -119,11 +121,18 @@ __global__ void __launch_bounds__(1024) qr_kernel(const CX* __restrict__ Ain, in
         for (int g = 0; g < QR_RG; ++g) w = cadd(w, part[g * QR_CG + cg]);
         const CX tw = cmul(t, w);
         for (int r = j + rg; r < M; r += QR_RG) {
-          CX* a = Q + r * qs_r + c * qs_c;
+          CX* a = Qf + r * qs_r + c * qs_c;
           *a = csub(*a, cmul(v[r], tw));
         }
       }
       __syncthreads();
+    }
+  }
+  if (trans_out) {
+    __syncthreads();
+    for (int64_t i = tid; i < (int64_t)M * kk; i += nt) {
+      const int c = (int)(i / M), r = (int)(i % M);  // coalesced writes of Q^T
+      Q[i] = Qf[(int64_t)r * kk + c];
     }
   }
 }
@@ -133,7 +142,7 @@ __global__ void __launch_bounds__(1024) qr_kernel(const CX* __restrict__ Ain, in
 extern "C" size_t agb_qr_workspace(int dtype, int M, int N) {
   const int esz = dtype == AGB_C64 ? 8 : 16;
   const int kk = M < N ? M : N;
-  return agb_align((size_t)M * N * esz) + agb_align((size_t)kk * esz);
+  return agb_align((size_t)M * N * esz) + agb_align((size_t)kk * esz) + agb_align((size_t)M * kk * esz);
 }
 
 extern "C" int agb_qr(int dtype, const void* A, int M, int N, int transA, void* Q, void* R,
@@ -147,16 +156,17 @@ extern "C" int agb_qr(int dtype, const void* A, int M, int N, int transA, void* 
   char* base = (char*)ws;
   void* W = base;
   void* tau = base + agb_align((size_t)M * N * esz);
+  void* Qw = (char*)tau + agb_align((size_t)kk * esz);
   const size_t smem = (size_t)M * esz + (size_t)QR_RG * QR_CG * esz;
   cudaStream_t s = (cudaStream_t)stream;
   if (dtype == AGB_C64) {
     if (smem > 48 * 1024) cudaFuncSetAttribute(qr_kernel<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     qr_kernel<float2><<<1, 1024, smem, s>>>((const float2*)A, M, N, transA, (float2*)W, (float2*)Q,
-                                             (float2*)R, trans_out, (float2*)tau);
+                                             (float2*)R, trans_out, (float2*)tau, (float2*)Qw);
   } else {
     if (smem > 48 * 1024) cudaFuncSetAttribute(qr_kernel<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     qr_kernel<double2><<<1, 1024, smem, s>>>((const double2*)A, M, N, transA, (double2*)W,
-                                              (double2*)Q, (double2*)R, trans_out, (double2*)tau);
+                                              (double2*)Q, (double2*)R, trans_out, (double2*)tau, (double2*)Qw);
   }
   (void)kk;
   AGB_CHECK_LAUNCH();
@@ -219,16 +229,18 @@ extern "C" int agb_qr_noalloc(int dtype, const void* A, int M, int N, int transA
   const int esz = dtype == AGB_C64 ? 8 : 16;
   void* W = base;
   void* tau = (char*)base + agb_align((size_t)M * N * esz);
+  const int kk = M < N ? M : N;
+  void* Qw = (char*)tau + agb_align((size_t)kk * esz);
   const size_t smem = (size_t)M * esz + (size_t)QR_RG * QR_CG * esz;
   cudaStream_t s = (cudaStream_t)stream;
   if (dtype == AGB_C64) {
     if (smem > 48 * 1024) cudaFuncSetAttribute(qr_kernel<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     qr_kernel<float2><<<1, 1024, smem, s>>>((const float2*)A, M, N, transA, (float2*)W, (float2*)Q,
-                                             (float2*)R, trans_out, (float2*)tau);
+                                             (float2*)R, trans_out, (float2*)tau, (float2*)Qw);
   } else {
     if (smem > 48 * 1024) cudaFuncSetAttribute(qr_kernel<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     qr_kernel<double2><<<1, 1024, smem, s>>>((const double2*)A, M, N, transA, (double2*)W,
-                                              (double2*)Q, (double2*)R, trans_out, (double2*)tau);
+                                              (double2*)Q, (double2*)R, trans_out, (double2*)tau, (double2*)Qw);
   }
   AGB_CHECK_LAUNCH();
   return AGB_OK;

@@ -34,7 +34,7 @@ namespace {
 
 AGB_DEV int row_offset(int i, int q, int C) { return i * (q + 1) + C * (i * (i - 1) / 2); }
 
-template <typename CX>
+template <typename CX, bool OVERFLOW>
 __global__ void __launch_bounds__(512, 1) tridiag_cluster_kernel(const HeevdProb* __restrict__ probs, int C,
                                                                  int cap_elems) {
   typedef typename cx_traits<CX>::R R;
@@ -64,8 +64,10 @@ __global__ void __launch_bounds__(512, 1) tridiag_cluster_kernel(const HeevdProb
   const int64_t ld = P.ldh;
   // own rows [0, isplit) are packed in shared memory, the rest live in H
   int isplit = 0;
-  while (isplit < nown && row_offset(isplit + 1, q, C) <= cap_elems) ++isplit;
+  if (OVERFLOW)
+    while (isplit < nown && row_offset(isplit + 1, q, C) <= cap_elems) ++isplit;
   auto rowp = [&](int i) -> CX* {
+    if (!OVERFLOW) return rows + row_offset(i, q, C);  // every row in shared memory
     return (i < isplit) ? rows + row_offset(i, q, C) : H + (int64_t)(q + i * C) * ld;
   };
   R* d = (R*)P.d;
@@ -266,9 +268,10 @@ int max_cluster(size_t smem) {
   int& c = cached[sizeof(CX) == 16][big];
   if (c >= 0) return c;
   c = 8;
-  if (cudaFuncSetAttribute(tridiag_cluster_kernel<CX>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+  if (cudaFuncSetAttribute(tridiag_cluster_kernel<CX, true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
       cudaSuccess) {
-    cudaFuncSetAttribute(tridiag_cluster_kernel<CX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBudget);
+    cudaFuncSetAttribute(tridiag_cluster_kernel<CX, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)kSmemBudget);
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(16, 1, 1);
     cfg.blockDim = dim3(512, 1, 1);
@@ -281,7 +284,8 @@ int max_cluster(size_t smem) {
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     int nclusters = 0;
-    if (cudaOccupancyMaxActiveClusters(&nclusters, tridiag_cluster_kernel<CX>, &cfg) == cudaSuccess && nclusters > 0)
+    if (cudaOccupancyMaxActiveClusters(&nclusters, tridiag_cluster_kernel<CX, true>, &cfg) == cudaSuccess &&
+        nclusters > 0)
       c = 16;
   }
   cudaGetLastError();
@@ -307,10 +311,12 @@ int launch_tridiag_cluster(const HeevdProb* probs, int count, int maxn, cudaStre
   const int C = tridiag_cluster_size(esz, maxn);
   if (C == 0) return AGB_ERR_UNSUPPORTED;
   size_t smem = tridiag_cluster_smem(esz, maxn, C);
-  if (smem > kSmemBudget) smem = kSmemBudget;
+  const bool overflow = smem > kSmemBudget;
+  if (overflow) smem = kSmemBudget;
   const int cap_elems = (int)(smem / esz) - 6 * maxn;
-  if (C > 8) cudaFuncSetAttribute(tridiag_cluster_kernel<CX>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-  cudaFuncSetAttribute(tridiag_cluster_kernel<CX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  auto kern = overflow ? tridiag_cluster_kernel<CX, true> : tridiag_cluster_kernel<CX, false>;
+  if (C > 8) cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(count * C, 1, 1);
   cfg.blockDim = dim3(512, 1, 1);
@@ -323,7 +329,7 @@ int launch_tridiag_cluster(const HeevdProb* probs, int count, int maxn, cudaStre
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  cudaError_t err = cudaLaunchKernelEx(&cfg, tridiag_cluster_kernel<CX>, probs, C, cap_elems);
+  cudaError_t err = cudaLaunchKernelEx(&cfg, kern, probs, C, cap_elems);
   agb_note_launch();
   if (err != cudaSuccess) return AGB_ERR_CUDA;
   return AGB_OK;

@@ -86,10 +86,31 @@ size_t tc_tail_bytes(int dtype, int ng, int maxm, int maxn, int maxell) {
 }
 
 // ------------------------------------------------------------------ setup
-__global__ void setup_kernel(const int64_t* __restrict__ desc, int ng, char* ws, int esz) {
+__global__ void setup_kernel(int64_t* __restrict__ desc, int ng, char* ws, int esz) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= ng) return;
-  const int64_t* D = desc + (int64_t)g * AGB_D_NFIELDS;
+  int64_t* D = desc + (int64_t)g * AGB_D_NFIELDS;
+  D[AGB_D_STATUS] = AGB_OK;
+  if (D[AGB_D_DIMS]) {
+    // device-resident MPS: the shapes are whatever earlier launches left in the
+    // bond-dimension array, bounded by the capacities the batch was planned
+    // with (CAPL/CAPM/CAPR, ELLPLAN stay untouched, so a captured launch
+    // sequence can be replayed)
+    const int* dims = (const int*)D[AGB_D_DIMS];
+    const int b = (int)D[AGB_D_BOND];
+    const int cL = dims[b], cM = dims[b + 1], cR = dims[b + 2];
+    const bool ok = cL >= 1 && cM >= 1 && cR >= 1 && cL <= (int)D[AGB_D_CAPL] && cM <= (int)D[AGB_D_CAPM] &&
+                    cR <= (int)D[AGB_D_CAPR];
+    D[AGB_D_CHIL] = ok ? cL : 1;  // 1 x 1 x 1: a shape every kernel handles
+    D[AGB_D_CHIM] = ok ? cM : 1;
+    D[AGB_D_CHIR] = ok ? cR : 1;
+    if (!ok) D[AGB_D_STATUS] = AGB_ERR_ARG;
+    const int mm = 2 * (int)D[AGB_D_CHIL], nn = 2 * (int)D[AGB_D_CHIR], cap = (int)D[AGB_D_CAP];
+    int full = mm < nn ? mm : nn;
+    if (cap < full) full = cap;
+    const int ep = (int)D[AGB_D_ELLPLAN];
+    D[AGB_D_ELL] = ep < full ? ep : full;
+  }
   const int chiL = (int)D[AGB_D_CHIL], chiM = (int)D[AGB_D_CHIM], chiR = (int)D[AGB_D_CHIR];
   const int m = 2 * chiL, n = 2 * chiR, ell = (int)D[AGB_D_ELL];
   char* slab = ws + D[AGB_D_WS];
@@ -107,6 +128,7 @@ __global__ void setup_kernel(const int64_t* __restrict__ desc, int ng, char* ws,
   p.ldv = ell;
   p.seed = (uint64_t)D[AGB_D_SEED];
   p.skip_vectors = 0;
+  p.nvec = ell;
   heevd_assign_scratch_dev(p, slab + L.heevd, esz);
   hp[g] = p;
   // gp[0..2ng) reserved for the eigensolver polish; [2ng, 3ng) Gram; [3ng, 4ng) AV
@@ -362,14 +384,27 @@ AGB_DEV void rank_rule_block(const double* s_sorted, double* E, int ell, int kma
   __syncthreads();
   int ktol = (sh_i[0] == 0x7fffffff) ? -1 : sh_i[0] + 1;
   const int full = min(kmax, cap);
-  if (ktol < 0) {
-    if (ell < full) {
+  if (ktol < 0 && ell < full) {
+    // Only the leading ell values are present.  If what is missing from the
+    // total is below the resolution of the rule (eps^2, or the float32 /
+    // float64 rounding of the total, whichever is larger), the cumulative sum
+    // has reached its final value inside the present values: k is where it
+    // stops changing, as in the full rule (where total is the cumsum's end).
+    const double res = fmax(eps * eps, f32 ? 1.2e-7 : 2.3e-16);
+    if (total_d - E[ell - 1] <= res * total_d) {
+      if (tid == 0) sh_i[1] = 0x7fffffff;
+      __syncthreads();
+      for (int t = tid; t < ell; t += nt)
+        if (E[t] >= E[ell - 1]) atomicMin(&sh_i[1], t);
+      __syncthreads();
+      ktol = sh_i[1] + 1;
+    } else {
       status = AGB_ERR_RANK;
       needed = full;
       ktol = ell;
-    } else {
-      ktol = kmax;
     }
+  } else if (ktol < 0) {
+    ktol = kmax;
   }
   ktol = min(ktol, kmax);
   k = min(min(ktol, cap), ell);
@@ -395,13 +430,21 @@ AGB_DEV void rank_rule_block(const double* s_sorted, double* E, int ell, int kma
   }
 }
 
-// Between the eigenvalue and eigenvector phases: when the rank rule keeps
-// every column (k == n <= m), any orthonormal basis factorises X exactly
-// (X = (X V)(V^H)), so the gate takes V = I: A_new = X, B_new = I.  This is a
-// unitary gauge change on the bond relative to the SVD factors, so the state
-// and every later gate's spectrum are unchanged.  Flat spectra (maximally
-// mixed small subsystems at the chain ends) would otherwise need one large
-// eigenvalue cluster orthogonalised.
+// Between the eigenvalue and eigenvector phases, with the eigenvalues of G:
+// * when the rank rule keeps every column (k == n <= m), any orthonormal basis
+//   factorises X exactly (X = (X V)(V^H)), so the gate takes V = I: A_new = X,
+//   B_new = I.  This is a unitary gauge change on the bond relative to the SVD
+//   factors, so the state and every later gate's spectrum are unchanged.  Flat
+//   spectra (maximally mixed small subsystems at the chain ends) would
+//   otherwise need one large eigenvalue cluster orthogonalised.
+// * otherwise only the eigenvectors the rank rule can keep are computed: the
+//   rule applied to the eigenvalues gives k_lam; the vector phase computes
+//   nvec = k_lam + pad (never splitting an eigenvalue cluster), and the rank
+//   kernel applies the rule again to the Rayleigh quotients of those vectors.
+//   If the threshold is not reached within nvec, the gate reports
+//   AGB_ERR_RANK and the caller re-runs it with every vector (NVEC = -1).
+//   Rank-deficient X (a zero eigenvalue of multiplicity n - rank) then costs
+//   nothing in the vector phase.
 template <typename CX>
 __global__ void prerank_kernel(int64_t* __restrict__ desc, int ng, char* ws) {
   typedef typename cx_traits<CX>::R R;
@@ -414,7 +457,9 @@ __global__ void prerank_kernel(int64_t* __restrict__ desc, int ng, char* ws) {
   GemmProb* gp = (GemmProb*)(ws + agb_align((size_t)ng * sizeof(HeevdProb)));
   D[AGB_D_MODE] = 0;
   hp[g].skip_vectors = 0;
-  if (m < n || ell != n || n > 1024) return;
+  hp[g].nvec = ell;
+  gp[3 * ng + g].N = ell;
+  if (n > 1024 || ell <= 0) return;
   const HeevdProb P = hp[g];
   const R* lam = (const R*)P.lam;
   const R scale = *((const R*)P.scale);
@@ -424,14 +469,35 @@ __global__ void prerank_kernel(int64_t* __restrict__ desc, int ng, char* ws) {
     const double a = v > R(0) ? (double)v : 0.0;
     s2[t] = (sizeof(R) == 4) ? (double)(float)a : a;
   }
+  // trace(G) = sum of the tridiagonal's diagonal (times the scale)
+  double tr = 0;
+  for (int i = 0; i < n; ++i) tr += (double)((const R*)P.d)[i];
+  tr *= (double)scale;
+  const int kmax = min(m, n);
   int k, status, needed;
   double el, en, cs;
-  rank_rule(s2, ell, min(m, n), cap, dbits(D[AGB_D_EPS]), sizeof(R) == 4, 0.0, k, el, en, cs, status, needed);
-  if (status == AGB_OK && k == n) {
+  rank_rule(s2, ell, kmax, cap, dbits(D[AGB_D_EPS]), sizeof(R) == 4, tr, k, el, en, cs, status, needed);
+  if (m >= n && ell == n && status == AGB_OK && k == n) {
     D[AGB_D_MODE] = 1;
     hp[g].skip_vectors = 1;
     gp[3 * ng + g].M = 0;  // no X*V product
+    return;
   }
+  if (D[AGB_D_NVEC] < 0 || status != AGB_OK) return;  // every vector
+  // k from the eigenvalues, then every eigenvalue above the float rounding
+  // level of G (values the rule on the Rayleigh quotients could still count),
+  // plus a pad for the difference between eigenvalues and Rayleigh quotients
+  int kl = k;
+  const double floor_ = s2[0] * (sizeof(R) == 4 ? 64.0 * 5.96e-8 : 64.0 * 1.11e-16);
+  while (kl < ell && s2[kl] > floor_) ++kl;
+  int nv = kl + max(8, kl / 8);
+  if (nv >= ell) return;
+  // do not split a cluster (the tolerance of the cluster kernel)
+  const R scl = fmax(fabs(lam[0]), fabs(lam[ell - 1]));
+  const R tol = (R)kClusterTolRel * fmax(scl, (R)(sizeof(R) == 4 ? 1e-30 : 1e-290));
+  while (nv < ell && (lam[nv - 1] - lam[nv]) <= tol) ++nv;
+  hp[g].nvec = nv;
+  gp[3 * ng + g].N = nv;
 }
 
 // ------------------------------------------------------------------ rank selection
@@ -468,22 +534,25 @@ __global__ void __launch_bounds__(1024) rank_kernel(int64_t* __restrict__ desc, 
   __syncthreads();
   const int mode0 = (int)D[AGB_D_MODE];
   const HeevdProb* hp = (const HeevdProb*)ws;
+  // values present: the nvec leading eigenvectors (all ell in the identity mode);
+  // AV and V keep the row stride ell
+  const int nv = (mode0 == 1) ? ell : min(hp[g].nvec, ell);
   // column norms of AV: lanes walk 32 consecutive columns (coalesced), warps
   // split the rows; partial sums meet in shared memory
-  for (int t = tid; t < ell; t += nt) s_raw[t] = 0.0;
+  for (int t = tid; t < nv; t += nt) s_raw[t] = 0.0;
   __syncthreads();
   if (mode0 != 1) {
     const int lane = tid & 31, wid = tid >> 5, nw = nt >> 5;
-    for (int c0 = 0; c0 < ell; c0 += 32) {
+    for (int c0 = 0; c0 < nv; c0 += 32) {
       const int t = c0 + lane;
-      if (t >= ell) continue;
+      if (t >= nv) continue;
       double acc = 0;
       for (int r = wid; r < m; r += nw) acc += (double)cabs2(AV[(int64_t)r * ell + t]);
       atomicAdd(&s_raw[t], acc);
     }
   }
   __syncthreads();
-  for (int t = tid; t < ell; t += nt) {
+  for (int t = tid; t < nv; t += nt) {
     double acc = s_raw[t];
     if (mode0 == 1) {
       // identity basis: the eigenvalues (descending) are the sigma^2
@@ -497,15 +566,15 @@ __global__ void __launch_bounds__(1024) rank_kernel(int64_t* __restrict__ desc, 
     s_raw[t] = f32 ? (double)(float)acc : acc;
   }
   __syncthreads();
-  // rank of each value (descending, ties by index): always a permutation of 0..ell-1.
+  // rank of each value (descending, ties by index): always a permutation of 0..nv-1.
   // The identity-basis mode keeps the eigenvalue order (already descending), so
   // the rank rule sees exactly the values the pre-rank decision used.
-  for (int t = tid; t < ell; t += nt) {
+  for (int t = tid; t < nv; t += nt) {
     const double v = s_raw[t];
     int rk = t;
     if (mode0 != 1) {
       rk = 0;
-      for (int u = 0; u < ell; ++u) {
+      for (int u = 0; u < nv; ++u) {
         const double w = s_raw[u];
         rk += (w > v) || (w == v && u < t);
       }
@@ -514,11 +583,11 @@ __global__ void __launch_bounds__(1024) rank_kernel(int64_t* __restrict__ desc, 
     perm[rk] = t;
   }
   __syncthreads();
-  for (int t = tid; t < ell; t += nt) sig2[t] = s_sorted[t];
+  for (int t = tid; t < nv; t += nt) sig2[t] = s_sorted[t];
   const int kmax = min(m, n);
   int k, status, needed;
   double eps_local, entropy, condS;
-  rank_rule_block(s_sorted, s_sorted + ell, ell, kmax, cap, eps, f32, total_d, k, eps_local, entropy, condS, status,
+  rank_rule_block(s_sorted, s_sorted + ell, nv, kmax, cap, eps, f32, total_d, k, eps_local, entropy, condS, status,
                   needed);
   if (tid != 0) return;
   if (nonfinite) {
@@ -527,6 +596,10 @@ __global__ void __launch_bounds__(1024) rank_kernel(int64_t* __restrict__ desc, 
   }
   if (*status_word(ws, ng) != 0) {  // a bounded wait in a tensor-core GEMM expired
     status = *status_word(ws, ng);
+    k = 0;
+  }
+  if (D[AGB_D_STATUS] != AGB_OK) {  // shapes rejected in setup
+    status = (int)D[AGB_D_STATUS];
     k = 0;
   }
   D[AGB_D_K] = k;
@@ -554,8 +627,12 @@ __global__ void scatter_kernel(const int64_t* __restrict__ desc, char* ws) {
   const int mode = (int)D[AGB_D_MODE];
   CX* An = (CX*)D[AGB_D_ANEW];
   CX* Bn = (CX*)D[AGB_D_BNEW];
-  if (!An || !Bn || k <= 0 || k > ell) return;
+  const int nv = (mode == 1) ? ell : min(((const HeevdProb*)ws)[g].nvec, ell);
+  if (!An || !Bn || k <= 0 || k > nv) return;
   if (mode == 1 && k != n) return;
+  if (D[AGB_D_STATUS] != AGB_OK) return;
+  if (D[AGB_D_DIMS] && blockIdx.x == 0 && threadIdx.x == 0)
+    ((int*)D[AGB_D_DIMS])[(int)D[AGB_D_BOND] + 1] = k;  // read by the next batch's setup
   const int64_t na = (int64_t)m * k, nb = (int64_t)k * n;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < na + nb;
        i += (int64_t)gridDim.x * blockDim.x) {
@@ -571,12 +648,12 @@ __global__ void scatter_kernel(const int64_t* __restrict__ desc, char* ws) {
     if (i < na) {
       const int r = (int)(i / k), j = (int)(i % k);
       const int pj = perm[j];
-      An[i] = (pj >= 0 && pj < ell) ? AV[(int64_t)r * ell + pj] : czero<CX>();
+      An[i] = (pj >= 0 && pj < nv) ? AV[(int64_t)r * ell + pj] : czero<CX>();
     } else {
       const int64_t ii = i - na;
       const int j = (int)(ii / n), c = (int)(ii % n);
       const int pj = perm[j];
-      Bn[ii] = (pj >= 0 && pj < ell) ? cconj(V[(int64_t)c * ell + pj]) : czero<CX>();
+      Bn[ii] = (pj >= 0 && pj < nv) ? cconj(V[(int64_t)c * ell + pj]) : czero<CX>();
     }
   }
 }
@@ -662,6 +739,12 @@ extern "C" int agb_two_site_plan(int dtype, int ng, int64_t* desc, size_t* ws_by
     int ell = (int)D[AGB_D_ELL];
     if (ell <= 0 || ell > full) ell = full;
     D[AGB_D_ELL] = ell;
+    if (D[AGB_D_DIMS]) {  // device-resident: the given shapes are capacities
+      D[AGB_D_CAPL] = chiL;
+      D[AGB_D_CAPM] = chiM;
+      D[AGB_D_CAPR] = chiR;
+      D[AGB_D_ELLPLAN] = ell;
+    }
     D[AGB_D_WS] = (int64_t)off;
     off += agb_align(slab_layout(m, n, ell, esz).total);
   }

@@ -12,7 +12,7 @@ Features (all O(1) on the host, per gate):
   1  log2(chi_R) / 10
   2  entangling power of the 4x4 gate (Zanardi, Zalka, Faoro 2000), scaled by 9/2 to [0, 1]
   3  mean entropy of the neighbouring bonds at their last update (nats) / 5
-  4  log2(previous rank of this bond) / 10
+  4  previous rank of this bond / min(2 chi_L, 2 chi_R, cap)
 Training, inference and the optimiser run on the GPU through the library's own
 kernels (agb_mlp_forward / agb_mlp_backward / agb_mlp_adam).
 
@@ -64,16 +64,16 @@ def gate_features(mps, gates):
         chiM = mps._tensors[i].shape[2]
         chiR = mps._tensors[i + 1].shape[2]
         nb = [ent[b] for b in (i - 1, i + 1) if b in ent]
-        X[g] = (math.log2(chiL) / 10.0, math.log2(chiR) / 10.0, ep[g] * 4.5,
-                (sum(nb) / len(nb) if nb else 0.0) / 5.0, math.log2(max(chiM, 1)) / 10.0)
         full[g] = min(2 * chiL, 2 * chiR, mps.chi_max_per_bond[i])
+        X[g] = (math.log2(chiL) / 10.0, math.log2(chiR) / 10.0, ep[g] * 4.5,
+                (sum(nb) / len(nb) if nb else 0.0) / 5.0, min(1.0, chiM / full[g]))
     return X, full
 
 
 class RankPredictor:
     """MLP on the GPU.  Call it as ``mps.rank_predictor = RankPredictor(...)``."""
 
-    def __init__(self, device="cuda", params=None, seed=0, margin=0.15, pad=8):
+    def __init__(self, device="cuda", params=None, seed=0, margin=0.1, pad=4):
         self.device = _lib.require_cuda(device)
         _lib.load()
         if params is None:
@@ -142,7 +142,7 @@ class RankPredictor:
 
     @classmethod
     def from_state_dict(cls, d, device="cuda"):
-        return cls(device=device, params=d["params"], margin=d.get("margin", 0.15), pad=d.get("pad", 8))
+        return cls(device=device, params=d["params"], margin=d.get("margin", 0.1), pad=d.get("pad", 4))
 
 
 def _init_params(seed):

@@ -111,11 +111,14 @@ def make_circuit():
     return haar_brickwork(N_QUBITS, DEPTH, seed=SEED)
 
 
-def run_ours(ops, device, dtype=torch.complex64):
+RESIDENT = True  # the headline runs the device-resident mode of the public API (set by --host-sync)
+
+
+def run_ours(ops, device, dtype=torch.complex64, resident=None):
     import atlasq_gb300 as aq
     pol = aq.DTypePolicy(default=dtype)
     m = aq.AdaptiveMPS(N_QUBITS, bond_dim=1, eps_bond=EPS, chi_max_per_bond=CHI, device=device,
-                       dtype=dtype, dtype_policy=pol)
+                       dtype=dtype, dtype_policy=pol, device_resident=RESIDENT if resident is None else resident)
     for _, q, U in ops:
         m.apply_two_site_gate(q, U)
     m.flush()
@@ -265,26 +268,48 @@ def secondary_workload(args):
             specs.append((n, chi, ops))
         ngates = sum(sum(1 for op in o if op[0] == "2q") for _, _, o in specs)
 
-        def one():
-            insts = [aq.AdaptiveMPS(n, bond_dim=1, eps_bond=1e-8, chi_max_per_bond=chi, device=device)
-                     for n, chi, _ in specs]
-            flush_buf.zero_()
-            (batch, ms) = _timed(lambda: aq.MPSBatch(insts).run([o for _, _, o in specs]), device)
-            return batch, insts, ms
+        def fresh(resident):
+            return [aq.AdaptiveMPS(n, bond_dim=1, eps_bond=1e-8, chi_max_per_bond=chi, device=device,
+                                   device_resident=resident) for n, chi, _ in specs]
+        # (1) host-synchronised batches (one ranks read-back per round)
+        insts = fresh(False)
+        flush_buf.zero_()
+        batch, ms_sync = _timed(lambda: aq.MPSBatch(insts).run([o for _, _, o in specs]), device)
+        ref_dims = [list(m.bond_dims) for m in insts]
+        # (2) device-resident, the whole 256-instance circuit captured as one CUDA graph
+        insts = fresh(True)
+        t0 = time.perf_counter()
+        cap = aq.MPSBatch(insts).capture([o for _, _, o in specs])
+        torch.cuda.synchronize()
+        capture_s = time.perf_counter() - t0
         for _ in range(args.warmup):
-            one()
+            cap.replay()
+        torch.cuda.synchronize()
         launches0 = lib.agb_launch_count()
         tot = 0.0
         for _ in range(args.steps):
-            batch, insts, ms = one()
-            tot += ms
+            flush_buf.zero_()
+            torch.cuda.synchronize()
+            s_, e_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s_.record(cap.stream)
+            cap.replay()
+            e_.record(cap.stream)
+            e_.synchronize()
+            tot += s_.elapsed_time(e_)
         ms = tot / args.steps
+        cap.finish()
+        same = sum(1 for m, d in zip(insts, ref_dims) if list(m.bond_dims) == d)
         line.update({"metric": "2-site gates/s, 256 HEA instances advanced together", "value": ngates / (ms / 1e3),
                      "unit": "gates/s", "ms_per_step": ms,
-                     "gpu_launches": (lib.agb_launch_count() - launches0) // max(args.steps, 1),
+                     "gpu_launches": cap.kernels_per_replay,
                      "config": {"workload": "256 HEA instances, n~U{16..48}, chi_max in {64,128,256}, 10 layers, eps 1e-8",
-                                "gates_per_step": ngates, "rounds_per_step": batch.rounds,
-                                "max_bond": max(max(m.bond_dims) for m in insts)}})
+                                "gates_per_step": ngates, "rounds_per_step": len(cap.rounds),
+                                "execution": "device-resident, whole circuit as one CUDA graph (replay timed)",
+                                "max_bond": max(max(m.bond_dims) for m in insts)},
+                     "host_synchronised": {"value": ngates / (ms_sync / 1e3), "unit": "gates/s",
+                                           "rounds": batch.rounds},
+                     "capture_seconds": capture_s,
+                     "instances_with_identical_bond_dims": same})
     elif args.workload == "sample50":
         from atlasq_gb300.sampling import right_canonical_copy, sample_tensors
         ops = [(k, q, U.to(device)) for k, q, U in haar_brickwork(50, 16, seed=77)]
@@ -370,9 +395,14 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--fp64-check", action="store_true", help="also run the complex128 GPU path and report fidelity")
+    ap.add_argument("--host-sync", action="store_true",
+                    help="run the host-synchronised mode (ranks read back after every batch) instead of the "
+                         "device-resident mode")
     ap.add_argument("--workload", default="brickwork40", choices=["brickwork40", "batch256", "sample50", "hea64"],
                     help="brickwork40 is the headline; the others are the secondary workloads")
     args = ap.parse_args()
+    global RESIDENT
+    RESIDENT = not args.host_sync
     if args.workload != "brickwork40" and args.impl == "ours":
         secondary_workload(args)
         return
@@ -442,8 +472,10 @@ def main():
     e2e_ms = max_over_ranks(dist, e2e_ms, device) / args.steps
     # per step: gate matrices (16 complex64) + two descriptor uploads per gate (32 int64 each);
     # back: one descriptor read per gate + the final site tensor
-    h2d = ngates * 16 * 8 + ngates * 2 * 32 * 8
-    d2h = ngates * 32 * 8 + res.numel() * res.element_size()
+    # host-synchronised: two descriptor uploads per gate (run, finalize), one read;
+    # resident: one upload per gate, the descriptors read once at the end (statistics)
+    h2d = ngates * 16 * 8 + ngates * (1 if RESIDENT else 2) * 32 * 8
+    d2h = ngates * 32 * 8 + res.numel() * res.element_size() + (4 * (N_QUBITS + 1) if RESIDENT else 0)
     e2e = {"value": ngates * ws / (e2e_ms / 1000.0), "unit": "gates/s", "h2d_bytes_per_step": h2d,
            "d2h_bytes_per_step": d2h}
 
@@ -500,7 +532,10 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "complex64", "data": "synthetic",
             "config": {"workload": WORKLOAD, "gates_per_step": ngates, "parallelism": f"replicas x{ws}",
-                       "l2": "flushed between timed steps (2x L2 write)", "precision": "fp32 SIMT + fp32 eigensolver"},
+                       "l2": "flushed between timed steps (2x L2 write)",
+                       "precision": "complex64; Gram / X.V / polish GEMMs on tcgen05 (3xTF32), FP32 eigensolver",
+                       "execution": "device-resident (no host sync between batches)" if RESIDENT else
+                                    "host-synchronised (ranks read back after every batch)"},
             "clocks": clocks, "gpu_launches": launches, "e2e": e2e, "roofline": roof}
 
     # ---------------------------------------------------------------- plain form on the same GPU

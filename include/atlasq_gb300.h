@@ -65,6 +65,21 @@ enum agb_desc_field {
   AGB_D_TOTAL = 21,   /* (out) ||X||_F^2 (double bits)                         */
   AGB_D_NEEDED = 22,  /* (out) eigenpairs actually required (fallback sizing)   */
   AGB_D_MODE = 23,    /* (out) 1: nothing truncated and m >= n, so A_new = X, B_new = I */
+  /* Device-resident MPS (optional).  With DIMS set, CHIL/CHIM/CHIR given to the
+   * plan are CAPACITIES; at run time the device reads the shapes from the
+   * instance's int32 bond-dimension array (site s is [dims[s], 2, dims[s+1]]),
+   * rewrites CHIL/CHIM/CHIR/ELL with them, and finalize writes dims[BOND+1] = k.
+   * A, B, ANEW, BNEW are then the capacity buffers of sites BOND, BOND+1
+   * (updated in place).  No host synchronisation is needed between batches, and
+   * a launch sequence over such descriptors can be captured and replayed. */
+  AGB_D_DIMS = 24,    /* (in)  int32* bond-dimension array, or 0              */
+  AGB_D_BOND = 25,    /* (in)  bond index i (with DIMS)                        */
+  AGB_D_CAPL = 26,    /* (plan) capacities recorded by the plan (with DIMS)    */
+  AGB_D_CAPM = 27,
+  AGB_D_CAPR = 28,
+  AGB_D_ELLPLAN = 29, /* (plan) planned eigenpair count (with DIMS)            */
+  AGB_D_NVEC = 30,    /* (in)  0: eigenvectors only for the values the rank rule can
+                       *       keep (from the eigenvalues, plus a pad); -1: all ell */
   AGB_D_NFIELDS = 32
 };
 
@@ -108,7 +123,8 @@ int agb_single_qubit_gate(int dtype, void* T, const void* U, int chiL, int chiR,
  * [ngroups][5] = {T, chiL, chiR, first, count} followed by the gate pointers
  * (2x2 matrices of the tensor's type); group g applies gates first..first+count-1
  * to T in order.  Groups must name distinct tensors.  max_elems >= chiL*chiR of
- * every group.  ngroups <= 65535. */
+ * every group.  ngroups <= 65535.  A device-resident tensor is given as
+ * {T, -1, (int64)&dims[site], first, count}: its shape is read on the device. */
 int agb_single_qubit_batch(int dtype, int ngroups, const int64_t* desc, int max_elems, void* stream);
 
 /* Hermitian eigensolver (batched), exposed for robust_svd / tests.
