@@ -10,7 +10,8 @@ rank_predictor.RankPredictor (learned kept-rank sizing)."""
 __version__ = "0.1.0"
 
 from .adaptive_mps import AdaptiveMPS, DTypePolicy, apply_gate_entries  # noqa: E402
-from .batched import MPSBatch  # noqa: E402
+from .batched import CapturedCircuit, MPSBatch  # noqa: E402
+from . import autotune  # noqa: E402
 from .diagnostics import MPSStatistics, bond_entropy_from_S, effective_rank, spectral_gap  # noqa: E402
 from .linalg_robust import condition_number, robust_qr, robust_svd  # noqa: E402
 from .mpo_ops import (MPO, MPOBuilder, correlation_function, expectation_value,  # noqa: E402

@@ -64,6 +64,9 @@ _SIGS = {
     "agb_two_site_finalize": (I, [I, I, P, I, I, I, P, P]),
     "agb_single_qubit_gate": (I, [I, P, P, I, I, P]),
     "agb_single_qubit_batch": (I, [I, I, P, I, P]),
+    "agb_tune_tridiag_workspace": (SZ, [I, I, I]),
+    "agb_tune_tridiag": (I, [I, I, I, P, SZ, P, P, P]),
+    "agb_tuned_tridiag_cluster": (I, [I, I, I]),
     "agb_heevd_workspace": (SZ, [I, I, I]),
     "agb_heevd": (I, [I, I, I, I, P, P, P, P, SZ, U64, P]),
     "agb_qr_workspace": (SZ, [I, I, I]),

@@ -160,6 +160,15 @@ class CapturedCircuit:
                 step["U2"] = U2
                 wsmax = max(wsmax, wsz)
             self.plan.append(step)
+        # autotune the eigensolver's cluster shape for the launches of this circuit
+        # (one tuning per size / batch-class, before anything is captured)
+        from .autotune import tune_for_batches
+        shapes = set()
+        for step in self.plan:
+            if "twos" in step:
+                _, _, dims, G, _ = step["twos"]
+                shapes.add((2 * dims[2], G))
+        self.tuned = tune_for_batches(sorted(shapes), dt, device)
         self.ws = torch.empty(wsmax, dtype=torch.uint8, device=device)
         self.stream = torch.cuda.Stream(device)
         self.stream.wait_stream(torch.cuda.current_stream(device))  # staged descriptors and gates
@@ -239,8 +248,10 @@ class CapturedCircuit:
         return self
 
     def replay(self):
-        """Run the captured circuit once (asynchronously on the capture stream)."""
-        self.graph.replay()
+        """Run the captured circuit once (asynchronously, ordered on the capture
+        stream; ``finish`` or ``stream.synchronize()`` waits for it)."""
+        with torch.cuda.stream(self.stream):
+            self.graph.replay()
         self.replays += 1
         return self
 

@@ -483,6 +483,109 @@ AGB_DEV R tri_solve(R* Y, int n, const R* U0, const R* U1, const R* U2, const R*
   return nrm;
 }
 
+// y <- (T - lam I)^{-1} (s * y) for column t of Y (stride L) with the stored
+// factors of column t; returns ||y||^2.  Factor and iterate loads do not depend
+// on the recurrence, so each chunk of IB steps loads them into registers first
+// (IB loads in flight instead of one dependent load per step).
+template <typename R>
+AGB_DEV R tri_solve_pf(R* Y, int n, const R* U0, const R* U1, const R* U2, const R* Lm, const R* Pv, int64_t L,
+                       int t, R piv, R s) {
+  constexpr int IB = 8;
+  R bi = Y[t] * s;
+  for (int i0 = 0; i0 < n - 1; i0 += IB) {
+    R yb[IB], pv[IB], lm[IB];
+#pragma unroll
+    for (int k = 0; k < IB; ++k) {
+      const int i = i0 + k;
+      if (i < n - 1) {
+        yb[k] = Y[(int64_t)(i + 1) * L + t];
+        pv[k] = Pv[(int64_t)i * L + t];
+        lm[k] = Lm[(int64_t)i * L + t];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < IB; ++k) {
+      const int i = i0 + k;
+      if (i < n - 1) {
+        R bn = yb[k] * s;
+        if (pv[k] != R(0)) {
+          const R tmp = bi;
+          bi = bn;
+          bn = tmp;
+        }
+        Y[(int64_t)i * L + t] = bi;
+        bi = bn - lm[k] * bi;
+      }
+    }
+  }
+  Y[(int64_t)(n - 1) * L + t] = bi;
+  R x1 = 0, x2 = 0, nrm = 0;
+  for (int i0 = n - 1; i0 >= 0; i0 -= IB) {
+    R u0[IB], u1[IB], u2[IB], yb[IB];
+#pragma unroll
+    for (int k = 0; k < IB; ++k) {
+      const int i = i0 - k;
+      if (i >= 0) {
+        u0[k] = U0[(int64_t)i * L + t];
+        u1[k] = U1[(int64_t)i * L + t];
+        u2[k] = U2[(int64_t)i * L + t];
+        yb[k] = Y[(int64_t)i * L + t];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < IB; ++k) {
+      const int i = i0 - k;
+      if (i >= 0) {
+        R u = u0[k];
+        if (fabs(u) < piv) u = copysign(piv, u == R(0) ? R(1) : u);
+        const R x = (yb[k] - u1[k] * x1 - u2[k] * x2) / u;
+        Y[(int64_t)i * L + t] = x;
+        nrm += x * x;
+        x2 = x1;
+        x1 = x;
+      }
+    }
+  }
+  return nrm;
+}
+
+// CGS2 of column jj of the staged cluster block Z (n x c, row-major in shared
+// memory) against its columns [0, jj), then normalisation (block-wide).
+template <typename R>
+AGB_DEV void cgs2_block_smem(R* Z, int n, int c, int jj, R* coef, R* red, R* part) {
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, wid = tid >> 5, nw = nt >> 5;
+  for (int pass = 0; pass < 2 && jj > 0; ++pass) {
+    for (int c0 = 0; c0 < jj; c0 += 32) {
+      const int i = c0 + lane;
+      R a = 0;
+      if (i < jj)
+        for (int r = wid; r < n; r += nw) a += Z[(int64_t)r * c + i] * Z[(int64_t)r * c + jj];
+      part[wid * 32 + lane] = a;
+      __syncthreads();
+      if (wid == 0 && i < jj) {
+        R sum = 0;
+        for (int w = 0; w < nw; ++w) sum += part[w * 32 + lane];
+        coef[i] = sum;
+      }
+      __syncthreads();
+    }
+    for (int r = wid; r < n; r += nw) {
+      R* row = Z + (int64_t)r * c;
+      R acc = 0;
+      for (int i = lane; i < jj; i += 32) acc += coef[i] * row[i];
+      acc = warp_sum(acc);
+      if (lane == 0) row[jj] -= acc;
+    }
+    __syncthreads();
+  }
+  R psum = 0;
+  for (int r = tid; r < n; r += nt) psum += Z[(int64_t)r * c + jj] * Z[(int64_t)r * c + jj];
+  const R nrm = block_sum(psum, red);
+  const R sc = R(1) / sqrt(fmax(nrm, rlim<R>::pivmin()));
+  for (int r = tid; r < n; r += nt) Z[(int64_t)r * c + jj] *= sc;
+  __syncthreads();
+}
+
 // CGS2 of the working column y (shared memory) against columns [t0, j) of Y
 // and normalisation (block-wide).  Dot products: tiles of 32 columns, lanes
 // over the columns (coalesced rows of Y), warps over row groups, partial sums
@@ -531,7 +634,8 @@ AGB_DEV void cgs2_normalize(R* y, const R* Y, int n, int64_t L, int t0, int j, R
 }
 
 template <typename R>
-__global__ void __launch_bounds__(256) cluster_invit_kernel(const HeevdProb* __restrict__ probs, double tolrel) {
+__global__ void __launch_bounds__(256) cluster_invit_kernel(const HeevdProb* __restrict__ probs, double tolrel,
+                                                            int zcap) {
   const HeevdProb P = probs[blockIdx.y];
   const int n = P.n, ell = P.ell, nv = P.nvec;
   if (nv < 2 || P.skip_vectors) return;
@@ -541,6 +645,7 @@ __global__ void __launch_bounds__(256) cluster_invit_kernel(const HeevdProb* __r
   R* coef = e + n;       // [ell]
   R* f = coef + ell;     // [5n] LU factors of the current member (U0,U1,U2,L,P)
   R* ycol = f + 5 * n;   // [n]  working column of the current member
+  R* Zs = ycol + n;      // [n * zcap] staged cluster block (parallel path)
   __shared__ int cl_t0, cl_t1;
   __shared__ R red[32];
   __shared__ R part[256];
@@ -591,6 +696,71 @@ __global__ void __launch_bounds__(256) cluster_invit_kernel(const HeevdProb* __r
   const R pert = R(10) * rlim<R>::eps() * fmax(tnorm, rlim<R>::pivmin());
   const int64_t L = ell;
   R* Y = (R*)P.Y;
+  const int c = t1 - t0;
+  if (c >= 3) {
+    // Members in parallel (LAPACK stein's iteration with the solves of all
+    // members at once): separated shifts; one LU per member (global, column j);
+    // two rounds of [solve every member; Gram-Schmidt in member order].
+    R* shs = f;  // [c] shifts (c <= ell <= 5n)
+    if (tid == 0) {
+      R pv = 0;
+      for (int j = t0; j < t1; ++j) {
+        R sh = lamg[j];
+        if (j > t0 && sh > pv - pert) sh = pv - pert;
+        shs[j - t0] = sh;
+        pv = sh;
+      }
+    }
+    __syncthreads();
+    R* lu = (R*)P.lu;
+    R* U0 = lu;
+    R* U1 = lu + (int64_t)n * L;
+    R* U2 = lu + 2 * (int64_t)n * L;
+    R* Lm = lu + 3 * (int64_t)n * L;
+    R* Pv = lu + 4 * (int64_t)n * L;
+    for (int j = t0 + tid; j < t1; j += nt) tri_lu(d, e, n, shs[j - t0], piv, U0, U1, U2, Lm, Pv, L, j);
+    for (int64_t idx = tid; idx < (int64_t)n * c; idx += nt) {
+      const int r = (int)(idx / c), j = t0 + (int)(idx % c);
+      Y[(int64_t)r * L + j] = (R)philox_normal(P.seed, (uint64_t)j * (uint64_t)n + r, 0x11u);
+    }
+    __syncthreads();
+    const bool staged = c <= zcap;
+    for (int it = 0; it < 2; ++it) {
+      for (int j = t0 + tid; j < t1; j += nt) {
+        const R nrm = tri_solve_pf(Y, n, U0, U1, U2, Lm, Pv, L, j, piv, R(1));
+        if (!(nrm < R(1e30)) || !(nrm > R(0)))  // breakdown: restart this member from a new random vector
+          for (int r = 0; r < n; ++r)
+            Y[(int64_t)r * L + j] = (R)philox_normal(P.seed ^ 0xABCDEFull, (uint64_t)(j + it + 1) * (uint64_t)n + r, 0x13u);
+        else {
+          const R sc = R(1) / sqrt(nrm);  // keep magnitudes O(1) for the float Gram-Schmidt
+          for (int r = 0; r < n; ++r) Y[(int64_t)r * L + j] *= sc;
+        }
+      }
+      __syncthreads();
+      if (staged) {
+        for (int64_t idx = tid; idx < (int64_t)n * c; idx += nt) {
+          const int r = (int)(idx / c), jj = (int)(idx % c);
+          Zs[idx] = Y[(int64_t)r * L + t0 + jj];
+        }
+        __syncthreads();
+        for (int jj = 0; jj < c; ++jj) cgs2_block_smem(Zs, n, c, jj, coef, red, part);
+        for (int64_t idx = tid; idx < (int64_t)n * c; idx += nt) {
+          const int r = (int)(idx / c), jj = (int)(idx % c);
+          Y[(int64_t)r * L + t0 + jj] = Zs[idx];
+        }
+        __syncthreads();
+      } else {
+        for (int j = t0; j < t1; ++j) {
+          for (int r = tid; r < n; r += nt) ycol[r] = Y[(int64_t)r * L + j];
+          __syncthreads();
+          cgs2_normalize(ycol, Y, n, L, t0, j, coef, red, part);
+          for (int r = tid; r < n; r += nt) Y[(int64_t)r * L + j] = ycol[r];
+          __syncthreads();
+        }
+      }
+    }
+    return;
+  }
   R prev = 0;
   for (int j = t0; j < t1; ++j) {
     if (tid == 0) {
@@ -766,11 +936,17 @@ int launch_heevd_vectors(HeevdProb* probs, GemmProb* gp, int count, int maxn, in
   AGB_CHECK_LAUNCH();
   prof_mark(AGB_ST_CLUSTER, s);
   {
-    const size_t sm = (8 * (size_t)maxn + (size_t)maxell) * sizeof(R);
+    // base: d, e, coef, 5n LU factors, a working column; then a staging area
+    // for the parallel path's cluster block (as many columns of n as fit)
+    const size_t base = (8 * (size_t)maxn + (size_t)maxell) * sizeof(R);
+    const size_t budget = 160 * 1024;
+    int zcap = base < budget ? (int)((budget - base) / ((size_t)maxn * sizeof(R))) : 0;
+    if (zcap > maxell) zcap = maxell;
+    const size_t sm = base + (size_t)zcap * maxn * sizeof(R);
     if (sm > 48 * 1024)
       cudaFuncSetAttribute(cluster_invit_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     const int maxcl = maxell / 2 > 0 ? maxell / 2 : 1;
-    cluster_invit_kernel<R><<<dim3(maxcl, count), 256, sm, s>>>(probs, kClusterTolRel);
+    cluster_invit_kernel<R><<<dim3(maxcl, count), 256, sm, s>>>(probs, kClusterTolRel, zcap);
     AGB_CHECK_LAUNCH();
   }
   int rc;

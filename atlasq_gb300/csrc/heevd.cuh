@@ -18,9 +18,10 @@
 
 // Eigenvalues closer than kClusterTolRel * max|lambda| are solved as a cluster
 // (re-orthogonalised inverse iteration).  Wider gaps leave inverse-iteration
-// vectors at most ~eps*||T||/gap (< 0.1 in float32) from orthogonal, which the
-// Newton-Schulz polish removes.
-constexpr double kClusterTolRel = 1e-6;
+// vectors close enough to orthogonal for the Newton-Schulz polish; 1e-6 is not
+// (a graded spectrum over eight decades left pairs 0.25 from orthogonal in
+// float32: the reduction to tridiagonal form itself carries n*eps*||G|| error).
+constexpr double kClusterTolRel = 1e-5;
 
 struct HeevdProb {
   void* H;       // CX[n x ldh], Hermitian input, overwritten by the reduction

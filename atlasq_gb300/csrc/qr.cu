@@ -11,6 +11,9 @@
 // Outputs: Q [M, kk] and R [kk, N] (upper triangular), or their transposes.
 #include "common.cuh"
 
+template <typename CX>
+int launch_qr_cluster(const CX* A, int M, int N, int transA, CX* Q, CX* R, int trans_out, CX* Qw, cudaStream_t s);
+
 namespace {
 
 constexpr int QR_CG = 128, QR_RG = 8;
@@ -159,6 +162,15 @@ extern "C" int agb_qr(int dtype, const void* A, int M, int N, int transA, void* 
   void* Qw = (char*)tau + agb_align((size_t)kk * esz);
   const size_t smem = (size_t)M * esz + (size_t)QR_RG * QR_CG * esz;
   cudaStream_t s = (cudaStream_t)stream;
+  // large matrices: the cluster kernel (columns in distributed shared memory)
+  if ((int64_t)M * N >= 64 * 64) {
+    const int rc = dtype == AGB_C64
+                       ? launch_qr_cluster<float2>((const float2*)A, M, N, transA, (float2*)Q, (float2*)R, trans_out,
+                                                   (float2*)Qw, s)
+                       : launch_qr_cluster<double2>((const double2*)A, M, N, transA, (double2*)Q, (double2*)R,
+                                                    trans_out, (double2*)Qw, s);
+    if (rc == AGB_OK) return AGB_OK;
+  }
   if (dtype == AGB_C64) {
     if (smem > 48 * 1024) cudaFuncSetAttribute(qr_kernel<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     qr_kernel<float2><<<1, 1024, smem, s>>>((const float2*)A, M, N, transA, (float2*)W, (float2*)Q,

@@ -293,10 +293,27 @@ int max_cluster(size_t smem) {
 }
 }  // namespace
 
-// Pick the cluster size for a matrix of size n: the smallest of 1..8 CTAs whose
-// shared memory holds every row (at least 8 above n = 256, where the per-step
-// work, not the barriers, dominates); else the largest cluster the device
-// schedules, with the overflow rows in L2.
+// Autotuned cluster sizes: [complex128][n bucket of 32][batch-count class], 0 = untuned.
+static int g_tuned_C[2][33][3] = {};
+
+static int count_class(int count) { return count <= 8 ? 0 : (count <= 32 ? 1 : 2); }
+
+static bool cluster_fits(int esz, int n, int C) {
+  if (C <= 8) return tridiag_cluster_smem(esz, n, C) <= kSmemBudget || C == 8;
+  return 6 * (size_t)n * esz + 64 * 1024 <= kSmemBudget;
+}
+
+// Pick the cluster size for a matrix of size n: the autotuned choice for this
+// size and batch class if there is one; otherwise the smallest of 1..8 CTAs
+// whose shared memory holds every row (at least 8 above n = 256, where the
+// per-step work, not the barriers, dominates); else the largest cluster the
+// device schedules, with the overflow rows in L2.
+int tridiag_cluster_size_for(int esz, int n, int count) {
+  const int t = g_tuned_C[esz == 16][(n + 31) / 32][count_class(count)];
+  if (t > 0 && cluster_fits(esz, n, t)) return t;
+  return tridiag_cluster_size(esz, n);
+}
+
 int tridiag_cluster_size(int esz, int n) {
   const int lo = n > 256 ? 8 : 1;
   for (int C = lo; C <= 8; ++C)
@@ -306,9 +323,16 @@ int tridiag_cluster_size(int esz, int n) {
 }
 
 template <typename CX>
+int launch_tridiag_cluster_C(const HeevdProb* probs, int count, int maxn, int C, cudaStream_t s);
+
+template <typename CX>
 int launch_tridiag_cluster(const HeevdProb* probs, int count, int maxn, cudaStream_t s) {
+  return launch_tridiag_cluster_C<CX>(probs, count, maxn, tridiag_cluster_size_for(sizeof(CX), maxn, count), s);
+}
+
+template <typename CX>
+int launch_tridiag_cluster_C(const HeevdProb* probs, int count, int maxn, int C, cudaStream_t s) {
   const int esz = sizeof(CX);
-  const int C = tridiag_cluster_size(esz, maxn);
   if (C == 0) return AGB_ERR_UNSUPPORTED;
   size_t smem = tridiag_cluster_smem(esz, maxn, C);
   const bool overflow = smem > kSmemBudget;
@@ -337,3 +361,110 @@ int launch_tridiag_cluster(const HeevdProb* probs, int count, int maxn, cudaStre
 
 template int launch_tridiag_cluster<float2>(const HeevdProb*, int, int, cudaStream_t);
 template int launch_tridiag_cluster<double2>(const HeevdProb*, int, int, cudaStream_t);
+
+// ---------------------------------------------------------------------------
+// Autotuner: time every admissible cluster size on `count` synthetic Hermitian
+// n x n problems (Philox Gaussian entries, the batch shape the pipeline will
+// launch) and remember the fastest for this size bucket and batch class.
+namespace {
+template <typename CX>
+__global__ void tune_fill_kernel(HeevdProb* probs, char* base, int count, int n, size_t stride, int esz,
+                                 uint64_t seed) {
+  const int b = blockIdx.y;
+  if (b >= count) return;
+  char* slab = base + (size_t)b * stride;
+  CX* H = (CX*)slab;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    HeevdProb p = {};
+    p.H = H;
+    p.ldh = n;
+    p.n = n;
+    p.ell = 1;
+    p.nvec = 1;
+    heevd_assign_scratch_dev(p, slab + agb_align((size_t)n * n * esz), esz);
+    probs[b] = p;
+  }
+  typedef typename cx_traits<CX>::R R;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (int64_t)n * n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int r = (int)(i / n), c = (int)(i % n);
+    const int lo = r < c ? r : c, hi = r < c ? c : r;
+    const uint64_t ctr = ((uint64_t)b * n + hi) * n + lo;
+    R re = (R)philox_normal(seed, ctr, 0x21u), im = (R)philox_normal(seed, ctr, 0x22u);
+    if (r == c) im = 0;
+    if (r < c) im = -im;
+    H[i] = mk<CX>(re, im);
+  }
+}
+
+template <typename CX>
+int tune_impl(int n, int count, void* ws, size_t ws_bytes, cudaStream_t s, int* best_C, float* best_ms) {
+  const int esz = sizeof(CX);
+  const size_t stride = agb_align((size_t)n * n * esz) + agb_align(heevd_scratch_bytes(esz, n, 1));
+  const size_t need = agb_align((size_t)count * sizeof(HeevdProb)) + (size_t)count * stride;
+  if (ws_bytes < need) return AGB_ERR_WORKSPACE;
+  HeevdProb* probs = (HeevdProb*)ws;
+  char* base = (char*)ws + agb_align((size_t)count * sizeof(HeevdProb));
+  int cands[8], nc = 0;
+  const int all[] = {1, 2, 4, 6, 8, 16};
+  const int maxC = tridiag_cluster_size(esz, n) > 8 ? 16 : 8;
+  for (int C : all)
+    if (C <= maxC && C <= n && cluster_fits(esz, n, C)) cands[nc++] = C;
+  cudaEvent_t e0, e1;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return AGB_ERR_CUDA;
+  int bC = 0;
+  float bms = 1e30f;
+  for (int k = 0; k < nc; ++k) {
+    float tot = 0;
+    for (int rep = 0; rep < 3; ++rep) {
+      tune_fill_kernel<CX><<<dim3(64, count), 256, 0, s>>>(probs, base, count, n, stride, esz, 1234 + rep);
+      cudaEventRecord(e0, s);
+      const int rc = launch_tridiag_cluster_C<CX>(probs, count, n, cands[k], s);
+      cudaEventRecord(e1, s);
+      if (rc != AGB_OK) {
+        cudaGetLastError();
+        tot = 1e30f;
+        break;
+      }
+      cudaEventSynchronize(e1);
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (rep > 0) tot += ms;  // first repetition warms up
+    }
+    if (tot < bms) {
+      bms = tot;
+      bC = cands[k];
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (cudaGetLastError() != cudaSuccess || bC == 0) return AGB_ERR_CUDA;
+  g_tuned_C[esz == 16][(n + 31) / 32][count_class(count)] = bC;
+  if (best_C) *best_C = bC;
+  if (best_ms) *best_ms = bms / 2;
+  return AGB_OK;
+}
+}  // namespace
+
+extern "C" size_t agb_tune_tridiag_workspace(int dtype, int n, int count) {
+  const int esz = dtype == AGB_C64 ? 8 : 16;
+  if (n <= 0 || count <= 0) return 0;
+  return agb_align((size_t)count * sizeof(HeevdProb)) +
+         (size_t)count * (agb_align((size_t)n * n * esz) + agb_align(heevd_scratch_bytes(esz, n, 1)));
+}
+
+extern "C" int agb_tune_tridiag(int dtype, int n, int count, void* ws, size_t ws_bytes, void* stream, int* best_C,
+                                float* best_ms) {
+  if (dtype != AGB_C64 && dtype != AGB_C128) return AGB_ERR_ARG;
+  if (n <= 1 || n > 1024 || count <= 0 || !ws) return AGB_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (dtype == AGB_C64) return tune_impl<float2>(n, count, ws, ws_bytes, s, best_C, best_ms);
+  return tune_impl<double2>(n, count, ws, ws_bytes, s, best_C, best_ms);
+}
+
+extern "C" int agb_tuned_tridiag_cluster(int dtype, int n, int count) {
+  if (dtype != AGB_C64 && dtype != AGB_C128) return -1;
+  if (n <= 0 || n > 1024 || count <= 0) return -1;
+  const int esz = dtype == AGB_C64 ? 8 : 16;
+  return tridiag_cluster_size_for(esz, n, count);
+}

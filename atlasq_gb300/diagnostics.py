@@ -32,7 +32,8 @@ def spectral_gap(S: torch.Tensor, k: int) -> float:
     return float((S[k - 1] / S[k]).item())
 
 
-GPU_DRIVERS = ("gb300_gram_heevd", "gb300_gram_heevd_full", "gb300_gram_heevd_c128")
+GPU_DRIVERS = ("gb300_gram_heevd", "gb300_gram_heevd_full", "gb300_gram_heevd_c128", "gb300_gram_heevd_resident",
+               "gb300_gram_heevd_unpromoted")
 
 
 class MPSStatistics:

@@ -35,6 +35,54 @@ from . import _lib, ops
 from ._lib import check, dtype_code, ptr, stream_ptr
 
 
+class _PinnedRing:
+    """Host->device uploads without host synchronisation: a ring of pinned
+    staging slots allocated once.  A slot is rewritten only after the copy that
+    last read it has completed (its event), so a fresh pinned allocation --
+    which synchronises the whole device -- never happens on the gate path."""
+
+    def __init__(self, device, nslots=128, slot_bytes=1 << 20):
+        self.device = device
+        self.slot_bytes = slot_bytes
+        self.slots = [torch.empty(slot_bytes, dtype=torch.uint8, pin_memory=True) for _ in range(nslots)]
+        self.views = [t.numpy() for t in self.slots]
+        self.events = [None] * nslots
+        self.next = 0
+
+    def upload(self, arr: np.ndarray) -> torch.Tensor:
+        raw = np.ascontiguousarray(arr).view(np.uint8).reshape(-1)
+        nb = raw.size
+        if nb > self.slot_bytes:  # rare: larger than a slot
+            return torch.from_numpy(np.ascontiguousarray(arr)).to(self.device)
+        i = self.next
+        self.next = (i + 1) % len(self.slots)
+        if self.events[i] is not None:
+            self.events[i].synchronize()
+        self.views[i][:nb] = raw
+        dev = torch.empty(nb, dtype=torch.uint8, device=self.device)
+        dev.copy_(self.slots[i][:nb], non_blocking=True)
+        ev = torch.cuda.Event()
+        ev.record(torch.cuda.current_stream(self.device))
+        self.events[i] = ev
+        return dev
+
+
+_rings = {}
+
+
+def upload(arr: np.ndarray, device, dtype=None, shape=None) -> torch.Tensor:
+    """Copy a host array to the device asynchronously (stream-ordered)."""
+    key = torch.device(device).index or 0
+    ring = _rings.get(key)
+    if ring is None:
+        ring = _rings[key] = _PinnedRing(torch.device(device))
+    dev = ring.upload(arr)
+    tdt = dtype if dtype is not None else {np.dtype(np.int64): torch.int64, np.dtype(np.complex64): torch.complex64,
+                                           np.dtype(np.complex128): torch.complex128}[np.dtype(arr.dtype)]
+    out = dev.view(tdt)
+    return out.reshape(shape if shape is not None else arr.shape)
+
+
 def _dbits(x: float) -> int:
     return int(np.array([x], dtype=np.float64).view(np.int64)[0])
 
@@ -139,12 +187,12 @@ def single_qubit_entries(entries):
                 host_slot.append(ng * 5 + first + j)
         first += len(Us)
     if host_U:
-        Ud = torch.stack(host_U).pin_memory().to(device, non_blocking=True)
+        Ud = upload(torch.stack(host_U).numpy(), device)
         keep.append(Ud)
         es = 4 * Ud.element_size()
         for j, slot in enumerate(host_slot):
             desc[slot] = Ud.data_ptr() + j * es
-    desc_dev = torch.from_numpy(desc).pin_memory().to(device, non_blocking=True)
+    desc_dev = upload(desc, device)
     check(lib.agb_single_qubit_batch(dtype_code(dt), ng, ptr(desc_dev), max_elems, stream_ptr(device)),
           "single_qubit_batch")
     for m, _, _ in groups.values():
@@ -190,7 +238,7 @@ def build_two_site(entries):
     check(lib.agb_two_site_plan(code, G, desc.ctypes.data_as(ctypes.c_void_p), ctypes.byref(wsz)), "two_site_plan")
     Ud = None
     if host_U:
-        Ud = torch.stack(host_U).pin_memory().to(device, non_blocking=True)
+        Ud = upload(torch.stack(host_U).numpy(), device)
         keep.append(Ud)
         for j, g in enumerate(host_rows):
             desc[g, _lib.D_U] = Ud.data_ptr() + j * 16 * Ud.element_size()
@@ -217,7 +265,7 @@ def two_site_entries(entries):
     device = m0.device
     desc, wsz, dims, keep = build_two_site(entries)
     ws = ops.workspace(wsz, device, "two_site_resident")
-    desc_dev = torch.from_numpy(desc).pin_memory().to(device, non_blocking=True)
+    desc_dev = upload(desc, device)
     launch_two_site(dtype_code(m0._res.dtype), len(entries), desc_dev, ws, wsz, dims, stream_ptr(device))
     t = time.perf_counter()
     rows = {}

@@ -127,6 +127,18 @@ int agb_single_qubit_gate(int dtype, void* T, const void* U, int chiL, int chiR,
  * {T, -1, (int64)&dims[site], first, count}: its shape is read on the device. */
 int agb_single_qubit_batch(int dtype, int ngroups, const int64_t* desc, int max_elems, void* stream);
 
+/* Autotuning of the Householder tridiagonalisation (the eigensolver's first
+ * stage): times every admissible thread-block-cluster size on `count`
+ * synthetic Hermitian n x n problems and keeps the fastest for this size
+ * (bucket of 32) and batch class (<= 8, <= 32, more problems per launch); later
+ * launches of that shape use it.  Synchronises the stream.  Returns the chosen
+ * size and its time per launch.  agb_tuned_tridiag_cluster reports the size
+ * currently used for a shape. */
+size_t agb_tune_tridiag_workspace(int dtype, int n, int count);
+int agb_tune_tridiag(int dtype, int n, int count, void* ws, size_t ws_bytes, void* stream, int* best_C,
+                     float* best_ms);
+int agb_tuned_tridiag_cluster(int dtype, int n, int count);
+
 /* Hermitian eigensolver (batched), exposed for robust_svd / tests.
  * Replaces the torch.linalg.svd call inside robust_svd (linalg_robust.py:37) when
  * used as X -> Gram -> eigenpairs.  H: [batch, n, n] Hermitian (overwritten);

@@ -451,3 +451,23 @@ def test_two_site_chi512_matches_svd(chiM, eps):
     assert f > 1 - 1e-6, f
     disc = np.sqrt(max(0.0, (S ** 2).sum() - (S[:k] ** 2).sum()))
     assert abs(m.statistics.logs["eps_local"][0] - disc) <= 1e-5 * S[0] + 1e-3 * disc
+
+
+def test_autotuned_cluster_shape_keeps_results():
+    """The autotuner picks an admissible cluster size, the library uses it for
+    that shape, and the eigensolver still meets its residual bound."""
+    from atlasq_gb300 import autotune
+    C, ms = autotune.tune_tridiag(300, 2)
+    assert C in (1, 2, 4, 6, 8, 16) and ms > 0
+    assert autotune.tuned_cluster(300, 2) == C
+    g = torch.Generator().manual_seed(77)
+    X = crandn(303, 300, gen=g, dtype=torch.complex128)
+    H = (X.conj().T @ X)
+    w, V = ops.heevd(torch.stack([H, H]).to(torch.complex64).to(DEV), ell=150)
+    ref = np.linalg.eigvalsh(H.numpy())[::-1][:150]
+    nrm = np.abs(ref).max()
+    for b in range(2):
+        wb = w[b].cpu().double().numpy()
+        Vb = V[b].cpu().to(torch.complex128).numpy()
+        assert np.max(np.abs(wb - ref)) <= 5e-5 * nrm
+        assert np.linalg.norm(H.numpy() @ Vb - Vb * wb[None, :]) <= 5e-5 * nrm * np.sqrt(150)
