@@ -124,6 +124,8 @@ def require_cuda(device):
     if dev.type != "cuda" or not torch.cuda.is_available():
         raise RuntimeError("atlasq_gb300 runs on a CUDA device only (GB300, sm_103a); "
                            f"got device={device!r}, cuda available={torch.cuda.is_available()}")
+    if dev.index is None:  # "cuda" -> "cuda:<current>", so device comparisons with tensors hold
+        dev = torch.device("cuda", torch.cuda.current_device())
     return dev
 
 

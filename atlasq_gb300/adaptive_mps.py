@@ -491,7 +491,9 @@ def apply_single_qubit_entries(entries):
         desc[5 * g:5 * g + 5] = (T.data_ptr(), T.shape[0], T.shape[2], first, len(Us))
         max_elems = max(max_elems, T.shape[0] * T.shape[2])
         for j, U in enumerate(Us):
-            if U.device == device and U.dtype == dt and U.is_contiguous():
+            if U.device == device:
+                if U.dtype != dt or not U.is_contiguous():
+                    U = U.to(dtype=dt).contiguous()  # device-side copy
                 keep.append(U)
                 desc[ng * 5 + first + j] = U.data_ptr()
             else:

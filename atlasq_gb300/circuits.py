@@ -27,7 +27,7 @@ def haar_unitary(gen, dim=4):
                       torch.randn(dim, dim, generator=gen, dtype=torch.float64)) / math.sqrt(2.0)
     q, r = torch.linalg.qr(z)
     d = torch.diagonal(r)
-    return (q * (d / torch.abs(d)).unsqueeze(0)).to(torch.complex64)
+    return (q * (d / torch.abs(d)).unsqueeze(0)).to(torch.complex64).contiguous()
 
 
 def ry(theta):

@@ -693,20 +693,20 @@ __global__ void __launch_bounds__(256) cluster_invit_kernel(const HeevdProb* __r
   for (int w = 0; w < (nt >> 5); ++w) tnorm = fmax(tnorm, red[w]);
   __syncthreads();
   const R piv = rlim<R>::eps() * fmax(tnorm, rlim<R>::pivmin());
-  const R pert = R(10) * rlim<R>::eps() * fmax(tnorm, rlim<R>::pivmin());
   const int64_t L = ell;
   R* Y = (R*)P.Y;
   const int c = t1 - t0;
   if (c >= 3) {
     // Members in parallel (LAPACK stein's iteration with the solves of all
     // members at once): separated shifts; one LU per member (global, column j);
-    // two rounds of [solve every member; Gram-Schmidt in member order].
+    // three rounds of [solve every member; Gram-Schmidt in member order].
     R* shs = f;  // [c] shifts (c <= ell <= 5n)
     if (tid == 0) {
       R pv = 0;
       for (int j = t0; j < t1; ++j) {
         R sh = lamg[j];
-        if (j > t0 && sh > pv - pert) sh = pv - pert;
+        const R pj = R(10) * rlim<R>::eps() * fmax(fabs(sh), rlim<R>::pivmin());
+        if (j > t0 && sh > pv - pj) sh = pv - pj;
         shs[j - t0] = sh;
         pv = sh;
       }
@@ -725,10 +725,10 @@ __global__ void __launch_bounds__(256) cluster_invit_kernel(const HeevdProb* __r
     }
     __syncthreads();
     const bool staged = c <= zcap;
-    for (int it = 0; it < 2; ++it) {
+    for (int it = 0; it < 3; ++it) {
       for (int j = t0 + tid; j < t1; j += nt) {
         const R nrm = tri_solve_pf(Y, n, U0, U1, U2, Lm, Pv, L, j, piv, R(1));
-        if (!(nrm < R(1e30)) || !(nrm > R(0)))  // breakdown: restart this member from a new random vector
+        if (!(nrm < R(1e300)) || !(nrm > R(0)))  // overflow / breakdown: restart from a new random vector
           for (int r = 0; r < n; ++r)
             Y[(int64_t)r * L + j] = (R)philox_normal(P.seed ^ 0xABCDEFull, (uint64_t)(j + it + 1) * (uint64_t)n + r, 0x13u);
         else {
@@ -765,7 +765,11 @@ __global__ void __launch_bounds__(256) cluster_invit_kernel(const HeevdProb* __r
   for (int j = t0; j < t1; ++j) {
     if (tid == 0) {
       R sh = lamg[j];
-      if (j > t0 && sh > prev - pert) sh = prev - pert;  // separate the shifts (descending)
+      // separate the shifts (descending) by a perturbation relative to the
+      // eigenvalue, as LAPACK's stein does: an absolute one (eps * ||T||) walks
+      // the shifts of a long run of small eigenvalues far below the cluster
+      const R pj = R(10) * rlim<R>::eps() * fmax(fabs(sh), rlim<R>::pivmin());
+      if (j > t0 && sh > prev - pj) sh = prev - pj;
       s_shift = sh;
       tri_lu(d, e, n, sh, piv, f, f + n, f + 2 * n, f + 3 * n, f + 4 * n, 1, 0);
     }

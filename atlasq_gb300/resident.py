@@ -179,7 +179,9 @@ def single_qubit_entries(entries):
         desc[5 * g:5 * g + 5] = (res.bufs[q].data_ptr(), -1, res.dims_ptr(q), first, len(Us))
         max_elems = max(max_elems, res.capL[q] * res.capR[q])
         for j, U in enumerate(Us):
-            if U.device == device and U.dtype == dt and U.is_contiguous():
+            if U.device == device:
+                if U.dtype != dt or not U.is_contiguous():
+                    U = U.to(dtype=dt).contiguous()  # device-side copy
                 keep.append(U)
                 desc[ng * 5 + first + j] = U.data_ptr()
             else:
@@ -217,7 +219,9 @@ def build_two_site(entries):
         row = desc[g]
         row[_lib.D_A] = row[_lib.D_ANEW] = res.bufs[i].data_ptr()
         row[_lib.D_B] = row[_lib.D_BNEW] = res.bufs[i + 1].data_ptr()
-        if U.device == device and U.dtype == dt and U.is_contiguous():
+        if U.device == device:
+            if U.dtype != dt or not U.is_contiguous():
+                U = U.to(dtype=dt).contiguous()  # a device-side copy, no synchronisation
             keep.append(U)
             row[_lib.D_U] = U.data_ptr()
         else:

@@ -111,7 +111,7 @@ def make_circuit():
     return haar_brickwork(N_QUBITS, DEPTH, seed=SEED)
 
 
-RESIDENT = True  # the headline runs the device-resident mode of the public API (set by --host-sync)
+RESIDENT = False  # the headline runs the default (host-synchronised) mode of the public API; --resident switches
 
 
 def run_ours(ops, device, dtype=torch.complex64, resident=None):
@@ -395,14 +395,14 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--fp64-check", action="store_true", help="also run the complex128 GPU path and report fidelity")
-    ap.add_argument("--host-sync", action="store_true",
-                    help="run the host-synchronised mode (ranks read back after every batch) instead of the "
-                         "device-resident mode")
+    ap.add_argument("--resident", action="store_true",
+                    help="run AdaptiveMPS(device_resident=True): no host synchronisation between batches")
+    ap.add_argument("--host-sync", action="store_true", help="the default mode (kept for scripts)")
     ap.add_argument("--workload", default="brickwork40", choices=["brickwork40", "batch256", "sample50", "hea64"],
                     help="brickwork40 is the headline; the others are the secondary workloads")
     args = ap.parse_args()
     global RESIDENT
-    RESIDENT = not args.host_sync
+    RESIDENT = bool(args.resident)
     if args.workload != "brickwork40" and args.impl == "ours":
         secondary_workload(args)
         return
