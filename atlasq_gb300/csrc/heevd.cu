@@ -856,10 +856,12 @@ __global__ void __launch_bounds__(WARPS * 32) backtransform2_kernel(const HeevdP
     const CX tj = tau[j];
     if (tj.x == R(0) && tj.y == R(0)) continue;
     CX s0 = czero<CX>(), s1 = czero<CX>();
+    // v_j is zero in rows <= j: chunks of 32 rows below that are skipped
+    // (a warp-uniform test, so the register arrays keep static indices)
 #pragma unroll
     for (int k = 0; k < NK; ++k) {
       const int r = lane + 32 * k;
-      if (r < n) {
+      if (32 * k + 31 > j && r < n) {
         const CX vr = buf[r];
         cfmac(s0, vr, z0[k]);
         cfmac(s1, vr, z1[k]);
@@ -870,7 +872,7 @@ __global__ void __launch_bounds__(WARPS * 32) backtransform2_kernel(const HeevdP
 #pragma unroll
     for (int k = 0; k < NK; ++k) {
       const int r = lane + 32 * k;
-      if (r < n) {
+      if (32 * k + 31 > j && r < n) {
         const CX vr = buf[r];
         z0[k] = csub(z0[k], cmul(vr, s0));
         z1[k] = csub(z1[k], cmul(vr, s1));

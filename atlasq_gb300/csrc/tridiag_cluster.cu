@@ -295,6 +295,7 @@ int max_cluster(size_t smem) {
 
 // Autotuned cluster sizes: [complex128][n bucket of 32][batch-count class], 0 = untuned.
 static int g_tuned_C[2][33][3] = {};
+static int g_tuned_T[2][33][3] = {};  // threads per CTA (256 or 512), 0 = 512
 
 static int count_class(int count) { return count <= 8 ? 0 : (count <= 32 ? 1 : 2); }
 
@@ -323,15 +324,19 @@ int tridiag_cluster_size(int esz, int n) {
 }
 
 template <typename CX>
-int launch_tridiag_cluster_C(const HeevdProb* probs, int count, int maxn, int C, cudaStream_t s);
+int launch_tridiag_cluster_C(const HeevdProb* probs, int count, int maxn, int C, cudaStream_t s, int threads = 512);
 
 template <typename CX>
 int launch_tridiag_cluster(const HeevdProb* probs, int count, int maxn, cudaStream_t s) {
-  return launch_tridiag_cluster_C<CX>(probs, count, maxn, tridiag_cluster_size_for(sizeof(CX), maxn, count), s);
+  const int C = tridiag_cluster_size_for(sizeof(CX), maxn, count);
+  const int tb = g_tuned_C[sizeof(CX) == 16][(maxn + 31) / 32][count_class(count)] == C
+                     ? g_tuned_T[sizeof(CX) == 16][(maxn + 31) / 32][count_class(count)]
+                     : 0;
+  return launch_tridiag_cluster_C<CX>(probs, count, maxn, C, s, tb > 0 ? tb : 512);
 }
 
 template <typename CX>
-int launch_tridiag_cluster_C(const HeevdProb* probs, int count, int maxn, int C, cudaStream_t s) {
+int launch_tridiag_cluster_C(const HeevdProb* probs, int count, int maxn, int C, cudaStream_t s, int threads) {
   const int esz = sizeof(CX);
   if (C == 0) return AGB_ERR_UNSUPPORTED;
   size_t smem = tridiag_cluster_smem(esz, maxn, C);
@@ -343,7 +348,7 @@ int launch_tridiag_cluster_C(const HeevdProb* probs, int count, int maxn, int C,
   cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(count * C, 1, 1);
-  cfg.blockDim = dim3(512, 1, 1);
+  cfg.blockDim = dim3(threads, 1, 1);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = s;
   cudaLaunchAttribute attr[1];
@@ -412,14 +417,15 @@ int tune_impl(int n, int count, void* ws, size_t ws_bytes, cudaStream_t s, int* 
     if (C <= maxC && C <= n && cluster_fits(esz, n, C)) cands[nc++] = C;
   cudaEvent_t e0, e1;
   if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return AGB_ERR_CUDA;
-  int bC = 0;
+  int bC = 0, bT = 512;
   float bms = 1e30f;
-  for (int k = 0; k < nc; ++k) {
+  for (int k = 0; k < 2 * nc; ++k) {
+    const int thr = (k & 1) ? 256 : 512;
     float tot = 0;
     for (int rep = 0; rep < 3; ++rep) {
       tune_fill_kernel<CX><<<dim3(64, count), 256, 0, s>>>(probs, base, count, n, stride, esz, 1234 + rep);
       cudaEventRecord(e0, s);
-      const int rc = launch_tridiag_cluster_C<CX>(probs, count, n, cands[k], s);
+      const int rc = launch_tridiag_cluster_C<CX>(probs, count, n, cands[k / 2], s, thr);
       cudaEventRecord(e1, s);
       if (rc != AGB_OK) {
         cudaGetLastError();
@@ -433,13 +439,15 @@ int tune_impl(int n, int count, void* ws, size_t ws_bytes, cudaStream_t s, int* 
     }
     if (tot < bms) {
       bms = tot;
-      bC = cands[k];
+      bC = cands[k / 2];
+      bT = thr;
     }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (cudaGetLastError() != cudaSuccess || bC == 0) return AGB_ERR_CUDA;
   g_tuned_C[esz == 16][(n + 31) / 32][count_class(count)] = bC;
+  g_tuned_T[esz == 16][(n + 31) / 32][count_class(count)] = bT;
   if (best_C) *best_C = bC;
   if (best_ms) *best_ms = bms / 2;
   return AGB_OK;
