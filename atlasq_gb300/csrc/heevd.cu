@@ -963,7 +963,11 @@ int launch_heevd_vectors(HeevdProb* probs, GemmProb* gp, int count, int maxn, in
   else rc = launch_bt<CX, 32>(probs, count, maxell, s);
   if (rc) return rc;
   prof_mark(AGB_ST_POLISH, s);
-  for (int step = 0; step < 4; ++step) {
+  // Newton-Schulz V <- V (3I - V^H V) / 2: quadratic convergence.  The vectors
+  // arrive within ~eps*||T||/gap of orthonormal (gaps below the cluster
+  // tolerance are handled by the cluster kernel), i.e. below ~1e-2 in float32,
+  // so two steps reach the float32 floor (an even count leaves the result in V).
+  for (int step = 0; step < 2; ++step) {
     polish_setup_kernel<<<(count + 127) / 128, 128, 0, s>>>(probs, gp, count, step & 1);
     AGB_CHECK_LAUNCH();
     if ((rc = launch_gemm_probs<CX>(gp, count, maxell, maxell, s, ctx, maxn))) return rc;
