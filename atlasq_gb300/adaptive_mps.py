@@ -73,6 +73,7 @@ class AdaptiveMPS:
             assert len(chi_max_per_bond) == num_qubits - 1, f"chi_max_per_bond must have length {num_qubits-1}"
             self.chi_max_per_bond = list(chi_max_per_bond)
         self._statistics = MPSStatistics()
+        self._log_queue = []
         self._operation_counter = 0
         self._seed = int(seed)
         self._pending = []
@@ -178,11 +179,16 @@ class AdaptiveMPS:
     @property
     def statistics(self) -> MPSStatistics:
         self._flush()
+        if self._log_queue:
+            q, self._log_queue = self._log_queue, []
+            for step, kw in q:
+                self._statistics.record(step=step, **kw)
         return self._statistics
 
     # ------------------------------------------------------------ stats API
     def _log_operation(self, **kwargs):
-        self._statistics.record(step=self._operation_counter, **kwargs)
+        # recorded when the statistics are read, off the gate path
+        self._log_queue.append((self._operation_counter, kwargs))
         self._operation_counter += 1
 
     def stats_summary(self) -> Dict[str, float]:
@@ -193,6 +199,7 @@ class AdaptiveMPS:
 
     def reset_stats(self):
         self.statistics.reset()
+        self._log_queue = []
         self._operation_counter = 0
 
     # ------------------------------------------------------------ gates
@@ -226,6 +233,13 @@ class AdaptiveMPS:
         self._pending.append((i, U))
         self._pending_sites.update((i, i + 1))
         self.is_canonical = False
+
+    def _eps_bits(self) -> int:
+        c = getattr(self, "_eps_cache", None)
+        if c is None or c[0] != self.eps_bond:
+            c = (self.eps_bond, _dbits(self.eps_bond))
+            self._eps_cache = c
+        return c[1]
 
     def _budget_ok_fn(self, chiL, chiM, chiR, dt):
         if self.budget_global_mb is None:
@@ -607,9 +621,9 @@ def _run_pipeline(entries, dt, ells, all_vectors=False):
         Us = Us.to(device, non_blocking=True)
     keep.append(Us)
     u_base, u_stride = Us.data_ptr(), 16 * Us.element_size()
-    maxL = maxM = maxR = 1
     meta = []
     seeds = {}
+    cols = {k: [0] * G for k in ("A", "B", "L", "M", "R", "cap", "eps", "seed")}
     for g, (m, i, _) in enumerate(entries):
         A = m._tensors[i]
         B = m._tensors[i + 1]
@@ -619,24 +633,29 @@ def _run_pipeline(entries, dt, ells, all_vectors=False):
             B = B.to(dt).contiguous()
         keep += [A, B]
         chiL, chiM, chiR = A.shape[0], A.shape[2], B.shape[2]
-        maxL, maxM, maxR = max(maxL, chiL), max(maxM, chiM), max(maxR, chiR)
-        # per-instance sketch seed: (instance seed, operation counter, position in its batch)
+        # per-instance seed: (instance seed, operation counter, position in its batch)
         j = seeds.get(id(m), 0)
         seeds[id(m)] = j + 1
-        seed = ((m._seed * 1000003 + m._operation_counter) & 0x3FFFFFFFFFFFFFFF) + j
-        row = desc[g]
-        row[_lib.D_A] = A.data_ptr()
-        row[_lib.D_B] = B.data_ptr()
-        row[_lib.D_U] = u_base + g * u_stride
-        row[_lib.D_CHIL] = chiL
-        row[_lib.D_CHIM] = chiM
-        row[_lib.D_CHIR] = chiR
-        row[_lib.D_CAP] = m.chi_max_per_bond[i]
-        row[_lib.D_EPS] = _dbits(m.eps_bond)
-        row[_lib.D_ELL] = int(ells[g]) if ells is not None else 0
-        row[_lib.D_SEED] = seed
-        row[_lib.D_NVEC] = -1 if all_vectors else 0
+        cols["A"][g] = A.data_ptr()
+        cols["B"][g] = B.data_ptr()
+        cols["L"][g], cols["M"][g], cols["R"][g] = chiL, chiM, chiR
+        cols["cap"][g] = m.chi_max_per_bond[i]
+        cols["eps"][g] = m._eps_bits()
+        cols["seed"][g] = ((m._seed * 1000003 + m._operation_counter) & 0x3FFFFFFFFFFFFFFF) + j
         meta.append((m, i, chiL, chiM, chiR))
+    desc[:, _lib.D_A] = cols["A"]
+    desc[:, _lib.D_B] = cols["B"]
+    desc[:, _lib.D_U] = u_base + np.arange(G, dtype=np.int64) * u_stride
+    desc[:, _lib.D_CHIL] = cols["L"]
+    desc[:, _lib.D_CHIM] = cols["M"]
+    desc[:, _lib.D_CHIR] = cols["R"]
+    desc[:, _lib.D_CAP] = cols["cap"]
+    desc[:, _lib.D_EPS] = cols["eps"]
+    if ells is not None:
+        desc[:, _lib.D_ELL] = [int(e) for e in ells]
+    desc[:, _lib.D_SEED] = cols["seed"]
+    desc[:, _lib.D_NVEC] = -1 if all_vectors else 0
+    maxL, maxM, maxR = max(cols["L"]), max(cols["M"]), max(cols["R"])
     wsz = _lib.SZ(0)
     check(lib.agb_two_site_plan(code, G, desc.ctypes.data_as(ctypes.c_void_p), ctypes.byref(wsz)),
           "two_site_plan")
@@ -649,14 +668,18 @@ def _run_pipeline(entries, dt, ells, all_vectors=False):
     out = desc_dev.cpu().numpy()
     res = []
     maxk = 1
+    sts = out[:, _lib.D_STATUS].tolist()
+    ks = out[:, _lib.D_K].tolist()
+    reals = np.ascontiguousarray(out[:, [_lib.D_EPSLOC, _lib.D_ENTROPY, _lib.D_CONDS]]).view(np.float64).tolist()
+    modes = out[:, _lib.D_MODE].tolist()
+    ellv = out[:, _lib.D_ELL].tolist()
     for g, (m, i, chiL, chiM, chiR) in enumerate(meta):
         row = out[g]
-        st = int(row[_lib.D_STATUS])
-        k = int(row[_lib.D_K])
-        r = {"status": st, "k": k, "eps_local": _bitsd(int(row[_lib.D_EPSLOC])),
-             "entropy": _bitsd(int(row[_lib.D_ENTROPY])), "condS": _bitsd(int(row[_lib.D_CONDS])),
+        st = sts[g]
+        k = ks[g]
+        r = {"status": st, "k": k, "eps_local": reals[g][0], "entropy": reals[g][1], "condS": reals[g][2],
              "chiL": chiL, "chiM": chiM, "chiR": chiR, "driver": "gb300_gram_heevd", "dtype": dt,
-             "mode": int(row[_lib.D_MODE]), "ell": int(row[_lib.D_ELL])}
+             "mode": modes[g], "ell": ellv[g]}
         if st not in (_lib.AGB_OK, _lib.AGB_ERR_RANK):
             check(st, f"two-site update on bond {i}")
         ok = m._budget_ok_fn(chiL, chiM, chiR, dt)
