@@ -23,6 +23,7 @@ AGB_ERR_TOO_LARGE = 8
 
 AGB_C64 = 0
 AGB_C128 = 1
+AGB_RUN_REPAIR = 1
 
 # descriptor fields (enum agb_desc_field)
 D_A, D_B, D_U, D_CHIL, D_CHIM, D_CHIR, D_CAP, D_EPS = 0, 1, 2, 3, 4, 5, 6, 7
@@ -60,7 +61,7 @@ _SIGS = {
     "agb_version": (I, []),
     "agb_contract_gate": (I, [I, P, P, P, P, I, I, I, P]),
     "agb_two_site_plan": (I, [I, I, P, ctypes.POINTER(SZ)]),
-    "agb_two_site_run": (I, [I, I, P, P, I, I, I, I, P, SZ, P]),
+    "agb_two_site_run": (I, [I, I, P, P, I, I, I, I, P, SZ, P, I]),
     "agb_two_site_finalize": (I, [I, I, P, I, I, I, P, P]),
     "agb_single_qubit_gate": (I, [I, P, P, I, I, P]),
     "agb_single_qubit_batch": (I, [I, I, P, I, P]),

@@ -663,8 +663,11 @@ def _run_pipeline(entries, dt, ells, all_vectors=False):
     ws = ops.workspace(wsz.value, device, "two_site")
     desc_dev = torch.from_numpy(desc).to(device)
     stream = stream_ptr(device)
+    # a gate whose eigenvalue-guided eigenvector count fell short is re-run with
+    # every vector on the device; AGB_ERR_RANK then only means a predicted ell
+    # below the rank, which the caller re-runs at full size
     check(lib.agb_two_site_run(code, G, ptr(desc_dev), ptr(desc_dev), maxL, maxM, maxR, maxell,
-                               ptr(ws), wsz.value, stream), "two_site_run")
+                               ptr(ws), wsz.value, stream, _lib.AGB_RUN_REPAIR), "two_site_run")
     out = desc_dev.cpu().numpy()
     res = []
     maxk = 1

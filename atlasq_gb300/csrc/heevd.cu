@@ -633,12 +633,47 @@ AGB_DEV void cgs2_normalize(R* y, const R* Y, int n, int64_t L, int t0, int j, R
   __syncthreads();
 }
 
+// Clusters of the leading nvec eigenvalues (consecutive gaps <= tol), once per
+// problem: P.M (the polish scratch, free until the polish) receives the count
+// and the (t0, t1) pairs.
+template <typename R>
+__global__ void cluster_list_kernel(const HeevdProb* __restrict__ probs, int count, double tolrel) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= count) return;
+  const HeevdProb P = probs[b];
+  int* clist = (int*)P.M;
+  const int ell = P.ell, nv = P.nvec;
+  if (nv < 2 || P.skip_vectors) {
+    clist[0] = 0;
+    return;
+  }
+  const R* lam = (const R*)P.lam;
+  const R tol = cluster_tol(lam, ell, tolrel);
+  int found = 0, s = 0;
+  for (int t = 1; t <= nv; ++t) {
+    if (t == nv || (lam[t - 1] - lam[t]) > tol) {
+      if (t - s > 1) {
+        clist[1 + 2 * found] = s;
+        clist[2 + 2 * found] = t;
+        ++found;
+      }
+      s = t;
+    }
+  }
+  clist[0] = found;
+}
+
 template <typename R>
 __global__ void __launch_bounds__(256) cluster_invit_kernel(const HeevdProb* __restrict__ probs, double tolrel,
                                                             int zcap) {
   const HeevdProb P = probs[blockIdx.y];
   const int n = P.n, ell = P.ell, nv = P.nvec;
   if (nv < 2 || P.skip_vectors) return;
+  // this CTA's cluster from the list cluster_list_kernel left in P.M
+  // (count, then (t0, t1) pairs): CTAs beyond the count exit at once
+  const int* clist = (const int*)P.M;
+  if ((int)blockIdx.x >= clist[0]) return;
+  const int t0 = clist[1 + 2 * blockIdx.x], t1 = clist[2 + 2 * blockIdx.x];
   extern __shared__ __align__(16) unsigned char smem_raw[];
   R* d = (R*)smem_raw;   // [n]
   R* e = d + n;          // [n]
@@ -646,38 +681,12 @@ __global__ void __launch_bounds__(256) cluster_invit_kernel(const HeevdProb* __r
   R* f = coef + ell;     // [5n] LU factors of the current member (U0,U1,U2,L,P)
   R* ycol = f + 5 * n;   // [n]  working column of the current member
   R* Zs = ycol + n;      // [n * zcap] staged cluster block (parallel path)
-  __shared__ int cl_t0, cl_t1;
   __shared__ R red[32];
   __shared__ R part[256];
   __shared__ R s_shift, s_nrm;
   const R* lamg = (const R*)P.lam;
   const int tid = threadIdx.x, nt = blockDim.x;
-  for (int t = tid; t < ell; t += nt) coef[t] = lamg[t];  // scan the eigenvalues from shared memory
-  __syncthreads();
-  const R* lam = coef;
-  if (tid == 0) {
-    const R tol = cluster_tol(lam, ell, tolrel);
-    int found = -1, s = 0, t0 = -1, t1 = -1;
-    for (int t = 1; t <= nv; ++t) {
-      if (t == nv || (lam[t - 1] - lam[t]) > tol) {
-        if (t - s > 1) {
-          ++found;
-          if (found == (int)blockIdx.x) {
-            t0 = s;
-            t1 = t;
-            break;
-          }
-        }
-        s = t;
-      }
-    }
-    cl_t0 = t0;
-    cl_t1 = t1;
-  }
-  __syncthreads();
-  const int t0 = cl_t0, t1 = cl_t1;
-  if (t0 < 0) return;
-  __syncthreads();  // the eigenvalue copy in coef is dead from here on
+  (void)tolrel;
   for (int i = tid; i < n; i += nt) {
     d[i] = ((const R*)P.d)[i];
     e[i] = (i < n - 1) ? ((const R*)P.e)[i] : R(0);
@@ -952,6 +961,8 @@ int launch_heevd_vectors(HeevdProb* probs, GemmProb* gp, int count, int maxn, in
     if (sm > 48 * 1024)
       cudaFuncSetAttribute(cluster_invit_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     const int maxcl = maxell / 2 > 0 ? maxell / 2 : 1;
+    cluster_list_kernel<R><<<(count + 127) / 128, 128, 0, s>>>(probs, count, kClusterTolRel);
+    AGB_CHECK_LAUNCH();
     cluster_invit_kernel<R><<<dim3(maxcl, count), 256, sm, s>>>(probs, kClusterTolRel, zcap);
     AGB_CHECK_LAUNCH();
   }
@@ -1007,6 +1018,7 @@ __global__ void heevd_setup_kernel(HeevdProb* probs, void* H, void* evecs, char*
   p.seed = seed + 0x9E3779B97F4A7C15ull * (uint64_t)b;
   p.skip_vectors = 0;
   p.nvec = ell;
+  p.redo = 0;
   heevd_assign_scratch_dev(p, scratch + (size_t)b * scratch_stride, esz);
   probs[b] = p;
 }

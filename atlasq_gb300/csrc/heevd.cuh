@@ -42,6 +42,7 @@ struct HeevdProb {
   int skip_vectors;  // set by the caller between the two phases: no eigenvectors needed
   int nvec;          // eigenvectors to compute (the leading nvec of the ell eigenvalues), <= ell;
                      // may be lowered between the two phases; strides stay ell
+  int redo;          // set by the two-site repair pass: this problem's vector phase runs again
 };
 
 // Bytes of per-problem scratch (d, e, tau, lam, Y, lu, V2, M, scale) for one

@@ -129,6 +129,7 @@ __global__ void setup_kernel(int64_t* __restrict__ desc, int ng, char* ws, int e
   p.seed = (uint64_t)D[AGB_D_SEED];
   p.skip_vectors = 0;
   p.nvec = ell;
+  p.redo = 0;
   heevd_assign_scratch_dev(p, slab + L.heevd, esz);
   hp[g] = p;
   // gp[0..2ng) reserved for the eigensolver polish; [2ng, 3ng) Gram; [3ng, 4ng) AV
@@ -506,10 +507,11 @@ __global__ void prerank_kernel(int64_t* __restrict__ desc, int ng, char* ws) {
 //   E = cumsum(S*S) accumulated in double, each partial rounded to float32;
 //   thresh = f32(f32(1 - eps^2) * total); k_tol = searchsorted_left(E, thresh) + 1.
 template <typename CX>
-__global__ void __launch_bounds__(1024) rank_kernel(int64_t* __restrict__ desc, int ng, char* ws) {
+__global__ void __launch_bounds__(1024) rank_kernel(int64_t* __restrict__ desc, int ng, char* ws, int only_redo) {
   typedef typename cx_traits<CX>::R R;
   const bool f32 = sizeof(R) == 4;
   const int g = blockIdx.x;
+  if (only_redo && !((const HeevdProb*)ws)[g].redo) return;
   int64_t* D = desc + (int64_t)g * AGB_D_NFIELDS;
   const int chiL = (int)D[AGB_D_CHIL], chiR = (int)D[AGB_D_CHIR];
   const int m = 2 * chiL, n = 2 * chiR, ell = (int)D[AGB_D_ELL], cap = (int)D[AGB_D_CAP];
@@ -658,9 +660,34 @@ __global__ void scatter_kernel(const int64_t* __restrict__ desc, char* ws) {
   }
 }
 
+// Repair pass (on the device, no host round trip): a gate whose eigenvector
+// phase was cut short by the eigenvalue-guided count (AGB_ERR_RANK with
+// nvec < ell) runs its vector phase, X*V and rank selection again with every
+// vector; every other gate is skipped by those launches.
+__global__ void repair_setup_kernel(int64_t* __restrict__ desc, int ng, char* ws) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= ng) return;
+  int64_t* D = desc + (int64_t)g * AGB_D_NFIELDS;
+  HeevdProb* hp = (HeevdProb*)ws;
+  GemmProb* gp = (GemmProb*)(ws + agb_align((size_t)ng * sizeof(HeevdProb)));
+  const int ell = (int)D[AGB_D_ELL];
+  if (D[AGB_D_STATUS] == AGB_ERR_RANK && hp[g].nvec < ell && D[AGB_D_MODE] == 0) {
+    hp[g].redo = 1;
+    hp[g].nvec = ell;
+    hp[g].skip_vectors = 0;
+    gp[3 * ng + g].N = ell;
+    gp[3 * ng + g].M = 2 * (int)D[AGB_D_CHIL];
+    D[AGB_D_STATUS] = AGB_OK;
+  } else {
+    hp[g].redo = 0;
+    hp[g].skip_vectors = 1;
+    gp[3 * ng + g].M = 0;
+  }
+}
+
 template <typename CX>
 int run_impl(int ng, int64_t* desc, int maxL, int maxM, int maxR, int maxell, char* ws, size_t ws_bytes,
-             size_t tc_bytes, cudaStream_t s) {
+             size_t tc_bytes, cudaStream_t s, int flags) {
   const int esz = sizeof(CX);
   if (cudaMemsetAsync(status_word(ws, ng), 0, sizeof(int), s) != cudaSuccess) return AGB_ERR_CUDA;
   prof_mark(AGB_ST_SETUP, s);
@@ -692,7 +719,22 @@ int run_impl(int ng, int64_t* desc, int maxL, int maxM, int maxR, int maxell, ch
   rc = launch_gemm_probs<CX>(gp + 3 * ng, ng, maxm, maxell, s, &ctx, maxn);
   if (rc) return rc;
   prof_mark(AGB_ST_RANK, s);
-  rank_kernel<CX><<<ng, 1024, 3 * (size_t)maxell * sizeof(double), s>>>(desc, ng, ws);
+  rank_kernel<CX><<<ng, 1024, 3 * (size_t)maxell * sizeof(double), s>>>(desc, ng, ws, 0);
+  AGB_CHECK_LAUNCH();
+  if (!(flags & AGB_RUN_REPAIR)) {
+    prof_mark(AGB_ST_GAP, s);
+    return AGB_OK;
+  }
+  // repair pass for gates whose guided eigenvector count was too small
+  repair_setup_kernel<<<(ng + 127) / 128, 128, 0, s>>>(desc, ng, ws);
+  AGB_CHECK_LAUNCH();
+  rc = launch_heevd_vectors<CX>(hp, gp, ng, maxn, maxell, s, &ctx);
+  if (rc) return rc;
+  prof_mark(AGB_ST_AV, s);
+  rc = launch_gemm_probs<CX>(gp + 3 * ng, ng, maxm, maxell, s, &ctx, maxn);
+  if (rc) return rc;
+  prof_mark(AGB_ST_RANK, s);
+  rank_kernel<CX><<<ng, 1024, 3 * (size_t)maxell * sizeof(double), s>>>(desc, ng, ws, 1);
   AGB_CHECK_LAUNCH();
   prof_mark(AGB_ST_GAP, s);
   return AGB_OK;
@@ -761,7 +803,7 @@ extern "C" int agb_two_site_plan(int dtype, int ng, int64_t* desc, size_t* ws_by
 
 extern "C" int agb_two_site_run(int dtype, int ng, const int64_t* desc_dev, int64_t* desc_out,
                                 int max_chiL, int max_chiM, int max_chiR, int max_ell, void* ws,
-                                size_t ws_bytes, void* stream) {
+                                size_t ws_bytes, void* stream, int flags) {
   (void)max_chiM;
   (void)desc_dev;
   if (dtype != AGB_C64 && dtype != AGB_C128) return AGB_ERR_ARG;
@@ -772,8 +814,9 @@ extern "C" int agb_two_site_run(int dtype, int ng, const int64_t* desc_dev, int6
   const size_t tc = tc_tail_bytes(dtype, ng, 2 * max_chiL, 2 * max_chiR, max_ell);
   cudaStream_t s = (cudaStream_t)stream;
   if (dtype == AGB_C64)
-    return run_impl<float2>(ng, desc_out, max_chiL, max_chiM, max_chiR, max_ell, (char*)ws, ws_bytes, tc, s);
-  return run_impl<double2>(ng, desc_out, max_chiL, max_chiM, max_chiR, max_ell, (char*)ws, ws_bytes, tc, s);
+    return run_impl<float2>(ng, desc_out, max_chiL, max_chiM, max_chiR, max_ell, (char*)ws, ws_bytes, tc, s, flags);
+  return run_impl<double2>(ng, desc_out, max_chiL, max_chiM, max_chiR, max_ell, (char*)ws, ws_bytes, tc, s,
+                           flags);
 }
 
 extern "C" int agb_two_site_finalize(int dtype, int ng, const int64_t* desc_dev, int max_chiL,

@@ -15,8 +15,9 @@ What a caller can observe:
   resident mode first (one synchronisation; the tensors become views of the
   capacity buffers, the per-gate statistics are read back then).
 * Kernel-side failures are reported at that point instead of at the gate.
-* Resident mode computes every eigenvector (no host fallback is available
-  mid-stream) and does not re-run ill-conditioned gates in complex128
+* A gate whose eigenvalue-guided eigenvector count falls short is re-run with
+  every vector on the device (the two-site repair pass), as the host path's
+  fallback would.  Resident mode does not re-run ill-conditioned gates in complex128
   (adaptive_mps.py:268-274 promotes when sigma_0 / sigma_{k-1} > 1e6); such gates
   are counted in ``AdaptiveMPS.unpromoted`` with the driver tag
   ``gb300_gram_heevd_unpromoted``.  In complex64 with eps_bond <= 1e-4 the kept
@@ -237,7 +238,7 @@ def build_two_site(entries):
         row[_lib.D_SEED] = ((m._seed * 1000003 + m._operation_counter + len(res.batches)) & 0x3FFFFFFFFFFFFFFF) + j
         row[_lib.D_DIMS] = res.dims.data_ptr()
         row[_lib.D_BOND] = i
-        row[_lib.D_NVEC] = -1
+        row[_lib.D_NVEC] = 0  # guided count; a short cut is repaired on the device
     wsz = _lib.SZ(0)
     check(lib.agb_two_site_plan(code, G, desc.ctypes.data_as(ctypes.c_void_p), ctypes.byref(wsz)), "two_site_plan")
     Ud = None
@@ -258,7 +259,7 @@ def launch_two_site(code, G, desc_dev, ws, wsz, dims, stream):
     lib = _lib.load()
     maxL, maxM, maxR, maxell, maxk = dims
     check(lib.agb_two_site_run(code, G, ptr(desc_dev), ptr(desc_dev), maxL, maxM, maxR, maxell, ptr(ws), wsz,
-                               stream), "two_site_run")
+                               stream, _lib.AGB_RUN_REPAIR), "two_site_run")
     check(lib.agb_two_site_finalize(code, G, ptr(desc_dev), maxL, maxR, min(maxk, 2 * max(maxL, maxR)), ptr(ws),
                                     stream), "two_site_finalize")
 

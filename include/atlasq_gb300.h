@@ -108,9 +108,12 @@ int agb_contract_gate(int dtype, const void* A, const void* B, const void* U, vo
  *                     adaptive_mps.py:281-285) and B_new = V_k^H into the
  *                     AGB_D_ANEW / AGB_D_BNEW buffers sized from AGB_D_K. */
 int agb_two_site_plan(int dtype, int ngates, int64_t* desc_host, size_t* ws_bytes);
+#define AGB_RUN_REPAIR 1 /* flags: re-run, on the device, the vector phase of gates whose
+                          * eigenvalue-guided eigenvector count fell short (AGB_D_NVEC = 0);
+                          * without it such gates report AGB_ERR_RANK to the caller */
 int agb_two_site_run(int dtype, int ngates, const int64_t* desc_dev, int64_t* desc_dev_out,
                      int max_chiL, int max_chiM, int max_chiR, int max_ell, void* ws, size_t ws_bytes,
-                     void* stream);
+                     void* stream, int flags);
 int agb_two_site_finalize(int dtype, int ngates, const int64_t* desc_dev, int max_chiL, int max_chiR,
                           int max_k, void* ws, void* stream);
 

@@ -162,3 +162,20 @@ def test_rank_predictor_gain_on_trotter_circuit():
     fa = sv.fidelity(plain.to_statevector().cpu().numpy(), exact)
     fb = sv.fidelity(pred.to_statevector().cpu().numpy(), exact)
     assert abs(fa - fb) <= 2e-3, (fa, fb)
+
+
+@pytest.mark.gpu
+def test_rank_fallback_reruns_match_plain_run():
+    """A predictor that always under-sizes (ell = 1) sends every truncating gate
+    through the re-run at full size: the state must equal the plain run's."""
+    from atlasq_gb300.circuits import trotter_ising
+    from oracle.mps_oracle import mps_fidelity
+    n, chi, eps = 12, 64, 1e-3
+    ops = trotter_ising(n, 10, 3)
+    plain = _run(ops, n, chi, eps)
+    low = _run(ops, n, chi, eps, predictor=lambda mps, gates: [1] * len(gates))
+    assert low.rank_fallbacks > 0
+    assert low.bond_dims == plain.bond_dims
+    ta = [t.cpu().numpy().astype(np.complex128) for t in plain.tensors]
+    tb = [t.cpu().numpy().astype(np.complex128) for t in low.tensors]
+    assert mps_fidelity(ta, tb) >= 1 - 1e-6
