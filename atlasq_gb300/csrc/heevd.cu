@@ -683,6 +683,7 @@ __global__ void __launch_bounds__(256) cluster_invit_kernel(const HeevdProb* __r
   R* Zs = ycol + n;      // [n * zcap] staged cluster block (parallel path)
   __shared__ R red[32];
   __shared__ R part[256];
+  __shared__ R ctile[32 * 32];  // blocked Gram-Schmidt coefficients (32 earlier members x block)
   __shared__ R s_shift, s_nrm;
   const R* lamg = (const R*)P.lam;
   const int tid = threadIdx.x, nt = blockDim.x;
@@ -759,11 +760,61 @@ __global__ void __launch_bounds__(256) cluster_invit_kernel(const HeevdProb* __r
         }
         __syncthreads();
       } else {
-        for (int j = t0; j < t1; ++j) {
-          for (int r = tid; r < n; r += nt) ycol[r] = Y[(int64_t)r * L + j];
+        // Blocked Gram-Schmidt for clusters wider than the staging area: blocks of
+        // B members are staged in shared memory, projected off every earlier member
+        // (tiles of 32 columns read from Y, twice), then orthonormalised inside the block.
+        const int B = zcap < 32 ? zcap : 32;  // ctile holds 32 x 32 coefficients
+        const int lane = tid & 31, wid = tid >> 5, nw = nt >> 5;
+        for (int b0 = t0; b0 < t1; b0 += B) {
+          const int bw = min(B, t1 - b0);
+          for (int64_t idx = tid; idx < (int64_t)n * bw; idx += nt) {
+            const int r = (int)(idx / bw), jj = (int)(idx % bw);
+            Zs[idx] = Y[(int64_t)r * L + b0 + jj];
+          }
           __syncthreads();
-          cgs2_normalize(ycol, Y, n, L, t0, j, coef, red, part);
-          for (int r = tid; r < n; r += nt) Y[(int64_t)r * L + j] = ycol[r];
+          for (int pass = 0; pass < 2 && b0 > t0; ++pass) {
+            for (int c0 = t0; c0 < b0; c0 += 32) {
+              const int tw = min(32, b0 - c0);
+              // coefficients ctile[i][jj] = Y[:, c0+i] . Z[:, jj]   (lanes over i: coalesced rows of Y)
+              for (int jj0 = 0; jj0 < bw; jj0 += 4 * nw) {
+                R acc[4] = {0, 0, 0, 0};
+                if (lane < tw) {
+                  for (int r = 0; r < n; ++r) {
+                    const R yv = Y[(int64_t)r * L + c0 + lane];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                      const int jj = jj0 + wid + u * nw;
+                      if (jj < bw) acc[u] += yv * Zs[(int64_t)r * bw + jj];
+                    }
+                  }
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                  const int jj = jj0 + wid + u * nw;
+                  if (jj < bw && lane < tw) ctile[lane * 32 + jj] = acc[u];
+                }
+              }
+              __syncthreads();
+              // Z[r][jj] -= sum_i Y[r, c0+i] ctile[i][jj]   (thread per row)
+              for (int r = tid; r < n; r += nt) {
+                R yr[32];
+#pragma unroll
+                for (int i = 0; i < 32; ++i) yr[i] = (i < tw) ? Y[(int64_t)r * L + c0 + i] : R(0);
+                for (int jj = 0; jj < bw; ++jj) {
+                  R a = 0;
+#pragma unroll
+                  for (int i = 0; i < 32; ++i) a += yr[i] * ctile[i * 32 + jj];
+                  Zs[(int64_t)r * bw + jj] -= a;
+                }
+              }
+              __syncthreads();
+            }
+          }
+          for (int jj = 0; jj < bw; ++jj) cgs2_block_smem(Zs, n, bw, jj, coef, red, part);
+          for (int64_t idx = tid; idx < (int64_t)n * bw; idx += nt) {
+            const int r = (int)(idx / bw), jj = (int)(idx % bw);
+            Y[(int64_t)r * L + b0 + jj] = Zs[idx];
+          }
           __syncthreads();
         }
       }
