@@ -709,7 +709,7 @@ __global__ void __launch_bounds__(256) cluster_invit_kernel(const HeevdProb* __r
   if (c >= 3) {
     // Members in parallel (LAPACK stein's iteration with the solves of all
     // members at once): separated shifts; one LU per member (global, column j);
-    // three rounds of [solve every member; Gram-Schmidt in member order].
+    // two rounds of [solve every member; Gram-Schmidt in member order].
     R* shs = f;  // [c] shifts (c <= ell <= 5n)
     if (tid == 0) {
       R pv = 0;
@@ -735,7 +735,7 @@ __global__ void __launch_bounds__(256) cluster_invit_kernel(const HeevdProb* __r
     }
     __syncthreads();
     const bool staged = c <= zcap;
-    for (int it = 0; it < 3; ++it) {
+    for (int it = 0; it < 2; ++it) {
       for (int j = t0 + tid; j < t1; j += nt) {
         const R nrm = tri_solve_pf(Y, n, U0, U1, U2, Lm, Pv, L, j, piv, R(1));
         if (!(nrm < R(1e300)) || !(nrm > R(0)))  // overflow / breakdown: restart from a new random vector
