@@ -323,7 +323,10 @@ __global__ void __launch_bounds__(128) invit_kernel(const HeevdProb* __restrict_
     Y[i * L + t] = b;
     nrm += b * b;
   }
-  for (int it = 0; it < 3; ++it) {
+  // two inverse-iteration solves from a random start: the shift is the
+  // bisection eigenvalue (error ~eps*||T||), so each solve amplifies the wanted
+  // component by ~gap/(eps*||T||) >= 1/(1e-5 tolerance ratio) over its neighbours
+  for (int it = 0; it < 2; ++it) {
     const R s = R(1) / sqrt(fmax(nrm, rlim<R>::pivmin()));
     // Forward (apply P and L) and backward substitution.  The factor and
     // iterate loads do not depend on the recurrence, so each chunk of IB steps
