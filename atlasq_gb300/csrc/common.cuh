@@ -60,6 +60,50 @@ template <typename CX> AGB_DEV CX warp_csum(CX v) {
   return v;
 }
 
+// Sum of float terms with double-precision accuracy.  The running sum is an
+// unevaluated pair hi + lo updated by Knuth's TwoSum (error-free: hi + x =
+// s + e exactly) and products enter through the FMA error-free product
+// (a * b = p + fma(a, b, -p) exactly), so the accumulation runs on the FP32
+// pipe.  GB300 issues about 2 FP64 operations per SM per clock, 64x fewer than
+// FP32, which makes plain double accumulation the bottleneck of any pass over
+// a matrix.  The double specialisation is plain double arithmetic.
+template <typename R> struct SumAcc;
+template <> struct SumAcc<float> {
+  float hi = 0.f, lo = 0.f;
+  AGB_DEV void merge(float x, float xlo) {
+    const float s = __fadd_rn(hi, x);
+    const float bp = __fsub_rn(s, hi);
+    const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(x, bp));
+    hi = s;
+    lo = __fadd_rn(__fadd_rn(lo, xlo), e);
+  }
+  AGB_DEV void add(float x) { merge(x, 0.f); }
+  AGB_DEV void add_prod(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    merge(p, fmaf(a, b, -p));
+  }
+  // every lane of the warp ends with the warp's total (TwoSum is exact, so
+  // both partners of a butterfly step compute the same pair)
+  AGB_DEV void warp_reduce() {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float h = __shfl_xor_sync(0xffffffffu, hi, o), l = __shfl_xor_sync(0xffffffffu, lo, o);
+      merge(h, l);
+    }
+  }
+  AGB_DEV double value() const { return (double)hi + (double)lo; }
+};
+template <> struct SumAcc<double> {
+  double s = 0.0;
+  AGB_DEV void add(double x) { s += x; }
+  AGB_DEV void add_prod(double a, double b) { s = fma(a, b, s); }
+  AGB_DEV void warp_reduce() {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  }
+  AGB_DEV double value() const { return s; }
+};
+
 // Block-wide sum of one value per thread; `red` must hold >= 32 entries.
 // All threads of the block must call it; every thread gets the result.
 template <typename T> AGB_DEV T block_sum(T v, T* red) {

@@ -25,24 +25,30 @@ __global__ void sample_site_kernel(const CX* __restrict__ temp, int shots, int c
   const int lane = threadIdx.x & 31;
   const int s = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (s >= shots) return;
+  typedef typename cx_traits<CX>::R R;
   const CX* row = temp + (int64_t)s * 2 * chiR;
-  double p0 = 0, p1 = 0;
+  // both probabilities to double accuracy on the FP32 pipe; the decision
+  // (double division, Philox) runs once per shot, in lane 0
+  SumAcc<R> a0, a1;
   for (int c = lane; c < chiR; c += 32) {
-    p0 += (double)cabs2(row[c]);
-    p1 += (double)cabs2(row[chiR + c]);
+    a0.add(cabs2(row[c]));
+    a1.add(cabs2(row[chiR + c]));
   }
-  p0 = warp_sum(p0) + 1e-15;
-  p1 = warp_sum(p1) + 1e-15;
-  const double pz = p0 / (p0 + p1);
-  const uint64_t shot = shot_offset + (uint64_t)s;
-  const philox_out o = philox4x32_10((uint32_t)shot, (uint32_t)(shot >> 32), (uint32_t)site, 0u,
-                                     (uint32_t)seed, (uint32_t)(seed >> 32));
-  const double u = (double)(o.x >> 8) * (1.0 / 16777216.0);
-  const int outc = (u >= pz) ? 1 : 0;
+  a0.warp_reduce();
+  a1.warp_reduce();
+  int outc = 0;
   if (lane == 0) {
+    const double p0 = a0.value() + 1e-15, p1 = a1.value() + 1e-15;
+    const double pz = p0 / (p0 + p1);
+    const uint64_t shot = shot_offset + (uint64_t)s;
+    const philox_out o = philox4x32_10((uint32_t)shot, (uint32_t)(shot >> 32), (uint32_t)site, 0u,
+                                       (uint32_t)seed, (uint32_t)(seed >> 32));
+    const double u = (double)(o.x >> 8) * (1.0 / 16777216.0);
+    outc = (u >= pz) ? 1 : 0;
     bits[s] = (bits[s] << 1) | outc;
     if (pz_out) pz_out[s] = pz;
   }
+  outc = __shfl_sync(0xffffffffu, outc, 0);
   if (Lnew) {
     const CX* src = row + outc * chiR;
     for (int c = lane; c < chiR; c += 32) Lnew[(int64_t)s * chiR + c] = src[c];
@@ -73,22 +79,49 @@ __global__ void mpo_mix_kernel(const CX* __restrict__ M, const CX* __restrict__ 
   }
 }
 
-// out = sum_{r,c} E[r,c] * Q[c,r]   (one block, double accumulation)
+// out = sum_{r,c} E[r,c] * Q[c,r]   (one block of 32 x 32 threads, double
+// accuracy).  32 x 32 tiles, two in flight per barrier: thread (ty, tx) takes
+// E[r0 + ty][c0 + tx] (coalesced) and Q[c0 + tx][r0 + ty] from a tile of Q
+// staged row-wise (coalesced) in shared memory.
 template <typename CX>
-__global__ void trace_prod_kernel(const CX* __restrict__ E, const CX* __restrict__ Q, int n, double* out) {
+__global__ void __launch_bounds__(1024) trace_prod_kernel(const CX* __restrict__ E, const CX* __restrict__ Q,
+                                                          int n, double* out) {
+  typedef typename cx_traits<CX>::R R;
+  __shared__ CX qs[2][32][33];
   __shared__ double red[32];
-  double re = 0, im = 0;
-  for (int64_t i = threadIdx.x; i < (int64_t)n * n; i += blockDim.x) {
-    const int r = (int)(i / n), c = (int)(i % n);
-    const CX a = E[i], b = Q[(int64_t)c * n + r];
-    re += (double)a.x * b.x - (double)a.y * b.y;
-    im += (double)a.x * b.y + (double)a.y * b.x;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int nb = (n + 31) / 32, ntile = nb * nb;
+  SumAcc<R> re, im;
+  for (int t0 = 0; t0 < ntile; t0 += 2) {
+    CX ev[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int t = t0 + u;
+      CX qv = czero<CX>();
+      ev[u] = czero<CX>();
+      if (t < ntile) {
+        const int r0 = (t / nb) * 32, c0 = (t % nb) * 32;
+        if (c0 + ty < n && r0 + tx < n) qv = Q[(int64_t)(c0 + ty) * n + r0 + tx];
+        if (r0 + ty < n && c0 + tx < n) ev[u] = E[(int64_t)(r0 + ty) * n + c0 + tx];
+      }
+      qs[u][ty][tx] = qv;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const CX a = ev[u], b = qs[u][tx][ty];
+      re.add_prod(a.x, b.x);
+      re.add_prod(-a.y, b.y);
+      im.add_prod(a.x, b.y);
+      im.add_prod(a.y, b.x);
+    }
+    __syncthreads();
   }
-  re = block_sum(re, red);
-  im = block_sum(im, red);
+  const double sre = block_sum(re.value(), red);
+  const double sim = block_sum(im.value(), red);
   if (threadIdx.x == 0) {
-    out[0] = re;
-    out[1] = im;
+    out[0] = sre;
+    out[1] = sim;
   }
 }
 

@@ -223,115 +223,18 @@ __global__ void __launch_bounds__(256) contract_gate_kernel(const ContractProb* 
     }
 }
 
-// The reference rank rule (truncation.py:21-83) on sigma^2 values sorted
-// descending, with torch-CPU float32 semantics when f32 (double-accumulated
-// cumsum rounded to float32 per element; threshold f32(f32(1 - eps^2) * total)).
-// total is E[-1] of the reference: our own cumsum end when every potentially
-// non-zero value is present (ell >= kmax), else ||X||_F^2.
-AGB_DEV void rank_rule(const double* s_sorted, int ell, int kmax, int cap, double eps, bool f32,
-                       double total_d, int& k, double& eps_local, double& entropy, double& condS,
-                       int& status, int& needed) {
-  eps_local = 0;
-  entropy = 0;
-  condS = INFINITY;
-  status = AGB_OK;
-  needed = ell;
-  if (ell == 0) {
-    k = 0;
-    return;
-  }
-  double total;
-  if (ell >= kmax) {
-    double a = 0;
-    for (int t = 0; t < ell; ++t) {
-      if (f32) {
-        const float s = sqrtf((float)s_sorted[t]);
-        a += (double)(s * s);
-      } else {
-        const double s = sqrt(s_sorted[t]);
-        a += s * s;
-      }
-    }
-    total = f32 ? (double)(float)a : a;
-  } else {
-    total = f32 ? (double)(float)total_d : total_d;
-  }
-  if (total < 1e-30) {
-    k = 1;
-    return;
-  }
-  double thresh;
-  if (f32) thresh = (double)(float)((float)(1.0 - eps * eps) * (float)total);
-  else thresh = (1.0 - eps * eps) * total;
-  double acc = 0;
-  int ktol = -1;
-  for (int t = 0; t < ell; ++t) {
-    double sq;
-    if (f32) {
-      const float sv = sqrtf((float)s_sorted[t]);
-      sq = (double)(sv * sv);
-    } else {
-      const double sv = sqrt(s_sorted[t]);
-      sq = sv * sv;
-    }
-    acc += sq;
-    const double Et = f32 ? (double)(float)acc : acc;
-    if (Et >= thresh) {
-      ktol = t + 1;
-      break;
-    }
-  }
-  const int full = min(kmax, cap);
-  if (ktol < 0) {
-    if (ell < full) {
-      status = AGB_ERR_RANK;
-      needed = full;
-      ktol = ell;
-    } else {
-      ktol = kmax;
-    }
-  }
-  ktol = min(ktol, kmax);
-  k = min(ktol, cap);
-  k = min(k, ell);
-  acc = 0;
-  for (int t = 0; t < k; ++t) {
-    if (f32) {
-      const float sv = sqrtf((float)s_sorted[t]);
-      acc += (double)(sv * sv);
-    } else {
-      const double sv = sqrt(s_sorted[t]);
-      acc += sv * sv;
-    }
-  }
-  const double Ek = f32 ? (double)(float)acc : acc;
-  const double rem = total - Ek;
-  eps_local = f32 ? (double)sqrtf((float)fmax(rem, 0.0)) : sqrt(fmax(rem, 0.0));
-  double ssum = 0;
-  for (int t = 0; t < k; ++t) ssum += s_sorted[t];
-  for (int t = 0; t < k; ++t) {
-    const double p = s_sorted[t] / ssum;
-    entropy -= p * log(fmax(p, 1e-30));
-  }
-  if (k > 1) {
-    if (f32) {
-      const float s0 = sqrtf((float)s_sorted[0]), sk = sqrtf((float)s_sorted[k - 1]);
-      condS = sk > 0.f ? (double)(s0 / sk) : INFINITY;
-    } else {
-      const double s0 = sqrt(s_sorted[0]), sk = sqrt(s_sorted[k - 1]);
-      condS = sk > 0 ? s0 / sk : INFINITY;
-    }
-  }
-}
-
-// Block-parallel form of rank_rule for one gate (all threads of the block call
-// it).  The float32 cumsum of the reference (double accumulation, each partial
-// rounded to float32) is a parallel double prefix sum; the first index reaching
-// the threshold is a block minimum; entropy terms are summed in parallel.  On
-// GB300 the serial double-precision loop costs ~0.6 ms per gate, this ~10 us.
+// The reference rank rule (truncation.py:21-83) for one gate, on sigma^2 values
+// sorted descending, with torch-CPU float32 semantics when f32 (double-
+// accumulated cumsum rounded to float32 per element; threshold
+// f32(f32(1 - eps^2) * total)).  total is E[-1] of the reference: the cumsum's
+// end when every potentially non-zero value is present (ell >= kmax), else
+// ||X||_F^2 (total_d).  All threads of the block call it: the cumsum is a
+// parallel double prefix sum, the first index reaching the threshold a block
+// minimum, the entropy terms a block sum (skipped when !stats).  On GB300 a
+// serial double-precision loop over the values costs ~0.6 ms per gate.
 AGB_DEV void rank_rule_block(const double* s_sorted, double* E, int ell, int kmax, int cap, double eps, bool f32,
                              double total_d, int& k, double& eps_local, double& entropy, double& condS,
-                             int& status, int& needed) {
+                             int& status, int& needed, bool stats = true) {
   __shared__ double sh_d[64];
   __shared__ int sh_i[4];
   __shared__ double sh_tot[2];
@@ -411,13 +314,24 @@ AGB_DEV void rank_rule_block(const double* s_sorted, double* E, int ell, int kma
   k = min(min(ktol, cap), ell);
   const double rem = total - E[k - 1];
   eps_local = f32 ? (double)sqrtf((float)fmax(rem, 0.0)) : sqrt(fmax(rem, 0.0));
+  if (!stats) return;
   double ssum = 0;
   for (int t = tid; t < k; t += nt) ssum += s_sorted[t];
   ssum = block_sum(ssum, sh_d);
+  // entropy terms in the working precision (float32 logs for complex64: the
+  // double-precision log is tens of FP64 operations per value)
   double ent = 0;
-  for (int t = tid; t < k; t += nt) {
-    const double pr = s_sorted[t] / ssum;
-    ent -= pr * log(fmax(pr, 1e-30));
+  if (f32) {
+    const float inv = 1.0f / (float)ssum;
+    for (int t = tid; t < k; t += nt) {
+      const float pr = (float)s_sorted[t] * inv;
+      ent -= (double)(pr * logf(fmaxf(pr, 1e-30f)));
+    }
+  } else {
+    for (int t = tid; t < k; t += nt) {
+      const double pr = s_sorted[t] / ssum;
+      ent -= pr * log(fmax(pr, 1e-30));
+    }
   }
   entropy = block_sum(ent, sh_d);
   if (k > 1) {
@@ -447,37 +361,41 @@ AGB_DEV void rank_rule_block(const double* s_sorted, double* E, int ell, int kma
 //   Rank-deficient X (a zero eigenvalue of multiplicity n - rank) then costs
 //   nothing in the vector phase.
 template <typename CX>
-__global__ void prerank_kernel(int64_t* __restrict__ desc, int ng, char* ws) {
+__global__ void __launch_bounds__(512) prerank_kernel(int64_t* __restrict__ desc, int ng, char* ws) {
   typedef typename cx_traits<CX>::R R;
-  const int g = blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= ng) return;
+  const int g = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
   int64_t* D = desc + (int64_t)g * AGB_D_NFIELDS;
   const int chiL = (int)D[AGB_D_CHIL], chiR = (int)D[AGB_D_CHIR];
   const int m = 2 * chiL, n = 2 * chiR, ell = (int)D[AGB_D_ELL], cap = (int)D[AGB_D_CAP];
   HeevdProb* hp = (HeevdProb*)ws;
   GemmProb* gp = (GemmProb*)(ws + agb_align((size_t)ng * sizeof(HeevdProb)));
-  D[AGB_D_MODE] = 0;
-  hp[g].skip_vectors = 0;
-  hp[g].nvec = ell;
-  gp[3 * ng + g].N = ell;
+  if (tid == 0) {
+    D[AGB_D_MODE] = 0;
+    hp[g].skip_vectors = 0;
+    hp[g].nvec = ell;
+    gp[3 * ng + g].N = ell;
+  }
   if (n > 1024 || ell <= 0) return;
   const HeevdProb P = hp[g];
   const R* lam = (const R*)P.lam;
   const R scale = *((const R*)P.scale);
-  double s2[1024];
-  for (int t = 0; t < ell; ++t) {
+  __shared__ double s2[1024], E[1024];
+  __shared__ double red[32];
+  for (int t = tid; t < ell; t += nt) {
     const R v = lam[t] * scale;
     const double a = v > R(0) ? (double)v : 0.0;
     s2[t] = (sizeof(R) == 4) ? (double)(float)a : a;
   }
   // trace(G) = sum of the tridiagonal's diagonal (times the scale)
-  double tr = 0;
-  for (int i = 0; i < n; ++i) tr += (double)((const R*)P.d)[i];
-  tr *= (double)scale;
+  SumAcc<R> ta;
+  for (int i = tid; i < n; i += nt) ta.add(((const R*)P.d)[i]);
+  const double tr = block_sum(ta.value(), red) * (double)scale;  // (ends with a barrier: s2 is complete)
   const int kmax = min(m, n);
   int k, status, needed;
   double el, en, cs;
-  rank_rule(s2, ell, kmax, cap, dbits(D[AGB_D_EPS]), sizeof(R) == 4, tr, k, el, en, cs, status, needed);
+  rank_rule_block(s2, E, ell, kmax, cap, dbits(D[AGB_D_EPS]), sizeof(R) == 4, tr, k, el, en, cs, status, needed,
+                  false);
+  if (tid != 0) return;
   if (m >= n && ell == n && status == AGB_OK && k == n) {
     D[AGB_D_MODE] = 1;
     hp[g].skip_vectors = 1;
@@ -526,11 +444,13 @@ __global__ void __launch_bounds__(1024) rank_kernel(int64_t* __restrict__ desc, 
   double* s_raw = (double*)smem_raw;  // [ell]
   double* s_sorted = s_raw + ell;     // [ell]
   __shared__ double red[32];
+  R* s_key = (R*)(s_sorted + 2 * (size_t)ell);  // [ell] sort keys (values are exact in R)
+  __shared__ double part[1024];
   const int tid = threadIdx.x, nt = blockDim.x;
-  // total = ||X||_F^2 in double
-  double part = 0;
-  for (int64_t i = tid; i < (int64_t)m * n; i += nt) part += (double)cabs2(X[i]);
-  const double total_d = block_sum(part, red);
+  // total = ||X||_F^2 to double accuracy
+  SumAcc<R> xa;
+  for (int64_t i = tid; i < (int64_t)m * n; i += nt) xa.add(cabs2(X[i]));
+  const double total_d = block_sum(xa.value(), red);
   __shared__ int nonfinite;
   if (tid == 0) nonfinite = !isfinite(total_d);
   __syncthreads();
@@ -539,21 +459,27 @@ __global__ void __launch_bounds__(1024) rank_kernel(int64_t* __restrict__ desc, 
   // values present: the nvec leading eigenvectors (all ell in the identity mode);
   // AV and V keep the row stride ell
   const int nv = (mode0 == 1) ? ell : min(hp[g].nvec, ell);
-  // column norms of AV: lanes walk 32 consecutive columns (coalesced), warps
-  // split the rows; partial sums meet in shared memory
-  for (int t = tid; t < nv; t += nt) s_raw[t] = 0.0;
-  __syncthreads();
+  // column norms of AV: a pass covers cw consecutive columns (one per thread,
+  // coalesced along the row); G = nt / cw groups of threads split the rows and
+  // group 0 adds the groups' partials in a fixed order
   if (mode0 != 1) {
-    const int lane = tid & 31, wid = tid >> 5, nw = nt >> 5;
-    for (int c0 = 0; c0 < nv; c0 += 32) {
-      const int t = c0 + lane;
-      if (t >= nv) continue;
-      double acc = 0;
-      for (int r = wid; r < m; r += nw) acc += (double)cabs2(AV[(int64_t)r * ell + t]);
-      atomicAdd(&s_raw[t], acc);
+    const int cw = min(max(32, ((nv + 31) / 32) * 32), nt), G = nt / cw;
+    const int lt = tid % cw, grp = tid / cw;
+    for (int c0 = 0; c0 < nv; c0 += cw) {
+      const int t = c0 + lt;
+      SumAcc<R> ca;
+      if (grp < G && t < nv)
+        for (int r = grp; r < m; r += G) ca.add(cabs2(AV[(int64_t)r * ell + t]));
+      part[tid] = ca.value();
+      __syncthreads();
+      if (grp == 0 && t < nv) {
+        double acc = 0;
+        for (int q = 0; q < G; ++q) acc += part[q * cw + lt];
+        s_raw[t] = acc;
+      }
+      __syncthreads();
     }
   }
-  __syncthreads();
   for (int t = tid; t < nv; t += nt) {
     double acc = s_raw[t];
     if (mode0 == 1) {
@@ -566,19 +492,23 @@ __global__ void __launch_bounds__(1024) rank_kernel(int64_t* __restrict__ desc, 
       acc = -1.0;  // sorts last; the gate is reported as failed below
     }
     s_raw[t] = f32 ? (double)(float)acc : acc;
+    s_key[t] = (R)s_raw[t];
   }
   __syncthreads();
   // rank of each value (descending, ties by index): always a permutation of 0..nv-1.
+  // The keys compare in R (exact: the values are rounded to R above), so the
+  // nv^2 comparisons stay off the FP64 pipe for complex64.
   // The identity-basis mode keeps the eigenvalue order (already descending), so
   // the rank rule sees exactly the values the pre-rank decision used.
   for (int t = tid; t < nv; t += nt) {
     const double v = s_raw[t];
     int rk = t;
     if (mode0 != 1) {
+      const R vk = s_key[t];
       rk = 0;
       for (int u = 0; u < nv; ++u) {
-        const double w = s_raw[u];
-        rk += (w > v) || (w == v && u < t);
+        const R w = s_key[u];
+        rk += (w > vk) || (w == vk && u < t);
       }
     }
     s_sorted[rk] = v;
@@ -711,7 +641,7 @@ int run_impl(int ng, int64_t* desc, int maxL, int maxM, int maxR, int maxell, ch
   if (rc) return rc;
   rc = launch_heevd_values<CX>(hp, ng, maxn, maxell, s);
   if (rc) return rc;
-  prerank_kernel<CX><<<(ng + 127) / 128, 128, 0, s>>>(desc, ng, ws);
+  prerank_kernel<CX><<<ng, 512, 0, s>>>(desc, ng, ws);
   AGB_CHECK_LAUNCH();
   rc = launch_heevd_vectors<CX>(hp, gp, ng, maxn, maxell, s, &ctx);
   if (rc) return rc;
@@ -719,7 +649,7 @@ int run_impl(int ng, int64_t* desc, int maxL, int maxM, int maxR, int maxell, ch
   rc = launch_gemm_probs<CX>(gp + 3 * ng, ng, maxm, maxell, s, &ctx, maxn);
   if (rc) return rc;
   prof_mark(AGB_ST_RANK, s);
-  rank_kernel<CX><<<ng, 1024, 3 * (size_t)maxell * sizeof(double), s>>>(desc, ng, ws, 0);
+  rank_kernel<CX><<<ng, 1024, 4 * (size_t)maxell * sizeof(double), s>>>(desc, ng, ws, 0);
   AGB_CHECK_LAUNCH();
   if (!(flags & AGB_RUN_REPAIR)) {
     prof_mark(AGB_ST_GAP, s);
@@ -734,7 +664,7 @@ int run_impl(int ng, int64_t* desc, int maxL, int maxM, int maxR, int maxell, ch
   rc = launch_gemm_probs<CX>(gp + 3 * ng, ng, maxm, maxell, s, &ctx, maxn);
   if (rc) return rc;
   prof_mark(AGB_ST_RANK, s);
-  rank_kernel<CX><<<ng, 1024, 3 * (size_t)maxell * sizeof(double), s>>>(desc, ng, ws, 1);
+  rank_kernel<CX><<<ng, 1024, 4 * (size_t)maxell * sizeof(double), s>>>(desc, ng, ws, 1);
   AGB_CHECK_LAUNCH();
   prof_mark(AGB_ST_GAP, s);
   return AGB_OK;
