@@ -910,13 +910,32 @@ __global__ void __launch_bounds__(WARPS * 32) backtransform2_kernel(const HeevdP
   }
   const CX* H = (const CX*)P.H;
   const CX* tau = (const CX*)P.tau;
+  // reflector j is read from global memory one step ahead (registers), so the
+  // L2 round trip overlaps the previous reflector's work instead of preceding
+  // every barrier; thread tid stages rows tid + WARPS * 32 * u
+  constexpr int PF = (NK * 32 + WARPS * 32 - 1) / (WARPS * 32);
+  CX pf[PF];
+  CX tnext = czero<CX>();
+  auto fetch = [&](int j) {
+    const CX* row = H + (int64_t)j * P.ldh;
+#pragma unroll
+    for (int u = 0; u < PF; ++u) {
+      const int r = tid + WARPS * 32 * u;
+      pf[u] = (r < n && r > j + 1) ? row[r] : czero<CX>();
+    }
+    tnext = tau[j];
+  };
+  if (n >= 2) fetch(n - 2);
   for (int j = n - 2; j >= 0; --j) {
     CX* buf = vbuf[j & 1];
-    const CX* row = H + (int64_t)j * P.ldh;
-    for (int r = tid; r < n; r += WARPS * 32)
-      buf[r] = (r <= j) ? czero<CX>() : (r == j + 1 ? mk<CX>(1, 0) : row[r]);
+#pragma unroll
+    for (int u = 0; u < PF; ++u) {
+      const int r = tid + WARPS * 32 * u;
+      if (r < n) buf[r] = (r == j + 1) ? mk<CX>(1, 0) : pf[u];
+    }
+    const CX tj = tnext;
+    if (j >= 1) fetch(j - 1);
     __syncthreads();
-    const CX tj = tau[j];
     if (tj.x == R(0) && tj.y == R(0)) continue;
     CX s0 = czero<CX>(), s1 = czero<CX>();
     // v_j is zero in rows <= j: chunks of 32 rows below that are skipped
