@@ -13,6 +13,10 @@
 
 template <typename CX>
 int launch_qr_cluster(const CX* A, int M, int N, int transA, CX* Q, CX* R, int trans_out, CX* Qw, cudaStream_t s);
+template <typename CX>
+int launch_qr_blocked(const CX* A, int M, int N, int transA, CX* Q, CX* R, int trans_out, void* ws, size_t ws_bytes,
+                      cudaStream_t s);
+size_t qr_blocked_workspace(int esz, int M, int N);
 
 namespace {
 
@@ -142,10 +146,17 @@ __global__ void __launch_bounds__(1024) qr_kernel(const CX* __restrict__ Ain, in
 
 }  // namespace
 
-extern "C" size_t agb_qr_workspace(int dtype, int M, int N) {
+// working copy of op(A), tau, column-major Q (single-CTA and unblocked cluster kernels)
+static size_t qr_unblocked_workspace(int dtype, int M, int N) {
   const int esz = dtype == AGB_C64 ? 8 : 16;
   const int kk = M < N ? M : N;
   return agb_align((size_t)M * N * esz) + agb_align((size_t)kk * esz) + agb_align((size_t)M * kk * esz);
+}
+
+extern "C" size_t agb_qr_workspace(int dtype, int M, int N) {
+  const size_t unblocked = qr_unblocked_workspace(dtype, M, N);
+  const size_t blocked = qr_blocked_workspace(dtype == AGB_C64 ? 8 : 16, M, N);
+  return unblocked > blocked ? unblocked : blocked;
 }
 
 extern "C" int agb_qr(int dtype, const void* A, int M, int N, int transA, void* Q, void* R,
@@ -162,8 +173,16 @@ extern "C" int agb_qr(int dtype, const void* A, int M, int N, int transA, void* 
   void* Qw = (char*)tau + agb_align((size_t)kk * esz);
   const size_t smem = (size_t)M * esz + (size_t)QR_RG * QR_CG * esz;
   cudaStream_t s = (cudaStream_t)stream;
-  // large matrices: the cluster kernel (columns in distributed shared memory)
+  // large matrices: the blocked cluster kernel (panels of reflectors, one
+  // cluster barrier per panel), else the unblocked one (columns in distributed
+  // shared memory)
   if ((int64_t)M * N >= 64 * 64) {
+    const int rb = dtype == AGB_C64
+                       ? launch_qr_blocked<float2>((const float2*)A, M, N, transA, (float2*)Q, (float2*)R, trans_out,
+                                                   ws, ws_bytes, s)
+                       : launch_qr_blocked<double2>((const double2*)A, M, N, transA, (double2*)Q, (double2*)R,
+                                                    trans_out, ws, ws_bytes, s);
+    if (rb == AGB_OK) return AGB_OK;
     const int rc = dtype == AGB_C64
                        ? launch_qr_cluster<float2>((const float2*)A, M, N, transA, (float2*)Q, (float2*)R, trans_out,
                                                    (float2*)Qw, s)
@@ -224,7 +243,7 @@ extern "C" int agb_qr_noalloc(int dtype, const void* A, int M, int N, int transA
   if (dtype != AGB_C64 && dtype != AGB_C128) return AGB_ERR_ARG;
   if (M <= 0 || N <= 0 || !A || !Q || !R) return AGB_ERR_ARG;
   if (M > 8192) return AGB_ERR_UNSUPPORTED;
-  const size_t need = agb_qr_workspace(dtype, M, N);
+  const size_t need = qr_unblocked_workspace(dtype, M, N);
   if (need > (size_t)AGB_QR_NOALLOC_MAX_BYTES) return AGB_ERR_TOO_LARGE;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return AGB_ERR_CUDA;
