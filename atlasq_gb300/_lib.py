@@ -76,6 +76,7 @@ _SIGS = {
     "agb_sample_site": (I, [I, P, I, I, I, U64, U64, P, P, P, P]),
     "agb_mpo_mix": (I, [I, P, P, P, I, I, I, I, P]),
     "agb_trace_prod": (I, [I, P, P, I, P, P]),
+    "agb_site_mix": (I, [I, P, P, P, I, I, I, P]),
     "agb_prof_begin": (I, [I]),
     "agb_launch_count": (ctypes.c_longlong, []),
     "agb_prof_end": (I, [P, P, I]),
@@ -86,6 +87,8 @@ _SIGS = {
     "agb_cgemm_tc_workspace": (SZ, [I, I, I, I]),
     "agb_cgemm_tc": (I, [ctypes.c_char, ctypes.c_char, I, I, I, I, P, I64, I64, P, I64, I64, P, I64, I64,
                          ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, P, SZ, P, P]),
+    "agb_cgemm_tc_async": (I, [ctypes.c_char, ctypes.c_char, I, I, I, I, P, I64, I64, P, I64, I64, P, I64, I64,
+                               ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, P, SZ, P, P]),
     "agb_cgemm_batched": (I, [I, ctypes.c_char, ctypes.c_char, I, I, I, I, P, I64, I64, P, I64, I64,
                               P, I64, I64, D, D, D, D, P]),
 }

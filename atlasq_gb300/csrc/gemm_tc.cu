@@ -393,10 +393,14 @@ extern "C" size_t agb_cgemm_tc_workspace(int batch, int M, int N, int K) {
   return agb_align((size_t)batch * sizeof(GemmProb)) + agb_align(sizeof(int)) + tc_gemm_scratch_bytes(batch, M, N, K);
 }
 
-extern "C" int agb_cgemm_tc(char opA, char opB, int batch, int M, int N, int K, const void* A, int64_t lda,
-                            int64_t strideA, const void* B, int64_t ldb, int64_t strideB, void* C, int64_t ldc,
-                            int64_t strideC, float alpha_re, float alpha_im, float beta_re, float beta_im, void* ws,
-                            size_t ws_bytes, int* status_host, void* stream) {
+// status_dev == NULL: the status word lives in the workspace, is cleared first,
+// and (if status_host) is read back after a stream synchronisation.
+// status_dev != NULL: the kernels record a timeout in *status_dev, which is
+// never cleared here (sticky across calls), and nothing synchronises.
+static int cgemm_tc_impl(char opA, char opB, int batch, int M, int N, int K, const void* A, int64_t lda,
+                         int64_t strideA, const void* B, int64_t ldb, int64_t strideB, void* C, int64_t ldc,
+                         int64_t strideC, float alpha_re, float alpha_im, float beta_re, float beta_im, void* ws,
+                         size_t ws_bytes, int* status_host, int* status_dev, void* stream) {
   const int oa = opc(opA), ob = opc(opB);
   if (oa < 0 || ob < 0 || batch < 0 || M < 0 || N < 0 || K <= 0 || !ws) return AGB_ERR_ARG;
   if (batch == 0 || M == 0 || N == 0) return AGB_OK;
@@ -424,15 +428,33 @@ extern "C" int agb_cgemm_tc(char opA, char opB, int batch, int M, int N, int K, 
   int* status = (int*)(w + agb_align((size_t)batch * sizeof(GemmProb)));
   void* scratch = w + agb_align((size_t)batch * sizeof(GemmProb)) + agb_align(sizeof(int));
   cudaStream_t s = (cudaStream_t)stream;
-  if (cudaMemsetAsync(status, 0, sizeof(int), s) != cudaSuccess) return AGB_ERR_CUDA;
+  if (status_dev) status = status_dev;
+  else if (cudaMemsetAsync(status, 0, sizeof(int), s) != cudaSuccess) return AGB_ERR_CUDA;
   strided_probs_kernel<<<(batch + 127) / 128, 128, 0, s>>>(probs, base, batch, strideA, strideB, strideC);
   AGB_CHECK_LAUNCH();
   int rc = launch_gemm_tc(probs, batch, M, N, K, scratch, ws_bytes - (size_t)((char*)scratch - w), status, s);
   if (rc) return rc;
-  if (status_host) {
+  if (status_host && !status_dev) {
     if (cudaMemcpyAsync(status_host, status, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess) return AGB_ERR_CUDA;
     if (cudaStreamSynchronize(s) != cudaSuccess) return AGB_ERR_CUDA;
     if (*status_host) return *status_host;
   }
   return AGB_OK;
+}
+
+extern "C" int agb_cgemm_tc(char opA, char opB, int batch, int M, int N, int K, const void* A, int64_t lda,
+                            int64_t strideA, const void* B, int64_t ldb, int64_t strideB, void* C, int64_t ldc,
+                            int64_t strideC, float alpha_re, float alpha_im, float beta_re, float beta_im, void* ws,
+                            size_t ws_bytes, int* status_host, void* stream) {
+  return cgemm_tc_impl(opA, opB, batch, M, N, K, A, lda, strideA, B, ldb, strideB, C, ldc, strideC, alpha_re,
+                       alpha_im, beta_re, beta_im, ws, ws_bytes, status_host, nullptr, stream);
+}
+
+extern "C" int agb_cgemm_tc_async(char opA, char opB, int batch, int M, int N, int K, const void* A, int64_t lda,
+                                  int64_t strideA, const void* B, int64_t ldb, int64_t strideB, void* C,
+                                  int64_t ldc, int64_t strideC, float alpha_re, float alpha_im, float beta_re,
+                                  float beta_im, void* ws, size_t ws_bytes, int* status_dev, void* stream) {
+  if (!status_dev) return AGB_ERR_ARG;
+  return cgemm_tc_impl(opA, opB, batch, M, N, K, A, lda, strideA, B, ldb, strideB, C, ldc, strideC, alpha_re,
+                       alpha_im, beta_re, beta_im, ws, ws_bytes, nullptr, status_dev, stream);
 }

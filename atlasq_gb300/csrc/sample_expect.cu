@@ -79,6 +79,30 @@ __global__ void mpo_mix_kernel(const CX* __restrict__ M, const CX* __restrict__ 
   }
 }
 
+// N[g][a][t][b] = sum_s W[g][s][t] M[g][a][s][b]   (W: one 2x2 operator per item)
+template <typename CX>
+__global__ void site_mix_kernel(const CX* __restrict__ M, const CX* __restrict__ W, CX* __restrict__ N, int count,
+                                int chiA, int chiB) {
+  const int64_t per = (int64_t)chiA * 2 * chiB;
+  const int g = blockIdx.y;
+  if (g >= count) return;
+  const CX w00 = W[g * 4 + 0], w01 = W[g * 4 + 1], w10 = W[g * 4 + 2], w11 = W[g * 4 + 3];
+  const CX* Mg = M + (int64_t)g * per;
+  CX* Ng = N + (int64_t)g * per;
+  const int64_t half = (int64_t)chiA * chiB;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < half; i += (int64_t)gridDim.x * blockDim.x) {
+    const int a = (int)(i / chiB), b = (int)(i % chiB);
+    const CX m0 = Mg[((int64_t)a * 2 + 0) * chiB + b], m1 = Mg[((int64_t)a * 2 + 1) * chiB + b];
+    CX n0 = czero<CX>(), n1 = czero<CX>();
+    cfma(n0, w00, m0);  // t = 0: W[0][0] M[s=0] + W[1][0] M[s=1]
+    cfma(n0, w10, m1);
+    cfma(n1, w01, m0);  // t = 1
+    cfma(n1, w11, m1);
+    Ng[((int64_t)a * 2 + 0) * chiB + b] = n0;
+    Ng[((int64_t)a * 2 + 1) * chiB + b] = n1;
+  }
+}
+
 // out = sum_{r,c} E[r,c] * Q[c,r]   (one block of 32 x 32 threads, double
 // accuracy).  32 x 32 tiles, two in flight per barrier: thread (ty, tx) takes
 // E[r0 + ty][c0 + tx] (coalesced) and Q[c0 + tx][r0 + ty] from a tile of Q
@@ -158,6 +182,25 @@ extern "C" int agb_mpo_mix(int dtype, const void* M, const void* W, void* N, int
     mpo_mix_kernel<float2><<<blocks, 256, 0, s>>>((const float2*)M, (const float2*)W, (float2*)N, Lw, Rw, chiA, chiB);
   else
     mpo_mix_kernel<double2><<<blocks, 256, 0, s>>>((const double2*)M, (const double2*)W, (double2*)N, Lw, Rw, chiA, chiB);
+  AGB_CHECK_LAUNCH();
+  return AGB_OK;
+}
+
+extern "C" int agb_site_mix(int dtype, const void* M, const void* W, void* N, int count, int chiA, int chiB,
+                            void* stream) {
+  if (dtype != AGB_C64 && dtype != AGB_C128) return AGB_ERR_ARG;
+  if (!M || !W || !N || count < 0 || count > 65535 || chiA <= 0 || chiB <= 0) return AGB_ERR_ARG;
+  if (count == 0) return AGB_OK;
+  const int64_t half = (int64_t)chiA * chiB;
+  int bx = (int)((half + 255) / 256);
+  if (bx > 256) bx = 256;
+  const dim3 grid(bx, count);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (dtype == AGB_C64)
+    site_mix_kernel<float2><<<grid, 256, 0, s>>>((const float2*)M, (const float2*)W, (float2*)N, count, chiA, chiB);
+  else
+    site_mix_kernel<double2><<<grid, 256, 0, s>>>((const double2*)M, (const double2*)W, (double2*)N, count, chiA,
+                                                  chiB);
   AGB_CHECK_LAUNCH();
   return AGB_OK;
 }

@@ -119,11 +119,23 @@ def _site_step(E, A, W):
     return out
 
 
+def _gemm(A, B, opA="N", opB="N"):
+    """complex64 products with every dimension >= 32 go to the tcgen05 GEMM
+    (3xTF32, float32 accuracy); the rest to the SIMT GEMM."""
+    ra, ca = A.shape[-2], A.shape[-1]
+    rb, cb = B.shape[-2], B.shape[-1]
+    M, K = (ra, ca) if opA == "N" else (ca, ra)
+    N = cb if opB == "N" else rb
+    if A.dtype == torch.complex64 and min(M, N, K) >= 32:
+        return ops.cgemm_tc(A, B, opA=opA, opB=opB, sync=False)
+    return ops.cgemm(A, B, opA=opA, opB=opB)
+
+
 def _norm_step(E, A):
     """Identity step: E' = sum_s A_s^H E A_s as two GEMMs (no mixing needed)."""
     chiA, _, chiB = A.shape
-    M = ops.cgemm(E, A.reshape(chiA, 2 * chiB))            # [chiA, 2chiB] == [(a,t), B] layout
-    return ops.cgemm(A.reshape(2 * chiA, chiB), M.reshape(2 * chiA, chiB), opA="C", opB="N")
+    M = _gemm(E, A.reshape(chiA, 2 * chiB))            # [chiA, 2chiB] == [(a,t), B] layout
+    return _gemm(A.reshape(2 * chiA, chiB), M.reshape(2 * chiA, chiB), opA="C", opB="N")
 
 
 @torch.no_grad()
@@ -140,7 +152,9 @@ def expectation_value(mpo: MPO, mps, use_gpu_optimized: bool = True) -> complex:
         A = tensors[i] if tensors[i].dtype == dt else tensors[i].to(dt).contiguous()
         E = _site_step(E, A, mpo.tensors[i])
         N = _norm_step(N, A)
-    return complex(E.reshape(-1)[0].item() / N.reshape(-1)[0].item())
+    val = complex(E.reshape(-1)[0].item() / N.reshape(-1)[0].item())
+    ops.check_tc_status(dev)
+    return val
 
 
 def correlation_function(op1: torch.Tensor, site1: int, op2: torch.Tensor, site2: int, mps) -> complex:
@@ -181,39 +195,66 @@ def environments(mps):
     for i in range(n - 1, -1, -1):
         A = tensors[i] if tensors[i].dtype == dt else tensors[i].to(dt).contiguous()
         chi, _, chi2 = A.shape
-        X = ops.cgemm(A.reshape(2 * chi, chi2), Renv[i + 1])          # [(B,s), r']
-        Renv[i] = ops.cgemm(X.reshape(chi, 2 * chi2), A.reshape(chi, 2 * chi2), opA="N", opB="C")
+        X = _gemm(A.reshape(2 * chi, chi2), Renv[i + 1])          # [(B,s), r']
+        Renv[i] = _gemm(X.reshape(chi, 2 * chi2), A.reshape(chi, 2 * chi2), opA="N", opB="C")
     return tensors, Lenv, Renv
 
 
 @torch.no_grad()
 def local_expectations(mps, observables: Sequence[Dict[int, torch.Tensor]]) -> List[complex]:
     """<psi|prod_i O_i^T|psi>/<psi|psi> for many product observables (site -> 2x2),
-    with the reference's transpose convention.  One left and one right sweep,
-    then each observable contracts only its support."""
+    with the reference's transpose convention (the per-site einsum of
+    expectation_value, src/atlas_q/mpo_ops.py:1145, with [1,2,2,1] MPO tensors).
+
+    One left and one right environment sweep; then every observable advances
+    one site of its support per round, starting from the left environment of
+    its first site: the items of a round whose site tensors have the same shape
+    share one batched GEMM pair (E A, then A^H (mixed E A)) and one site-mix
+    launch (agb_site_mix; sites inside the support without an operator mix with
+    the identity).  Each finished item is closed with the right environment."""
     lib = _lib.load()
     tensors, Lenv, Renv = environments(mps)
     dt = tensors[0].dtype
     dev = tensors[0].device
     code = dtype_code(dt)
-    out2 = torch.zeros(len(observables) + 1, 2, dtype=torch.float64, device=dev)
+    nobs = len(observables)
+    out2 = torch.zeros(nobs + 1, 2, dtype=torch.float64, device=dev)
     stream = stream_ptr(dev)
     # norm = tr(Lenv[n]) (1x1)
     check(lib.agb_trace_prod(code, ptr(Lenv[-1]), ptr(Renv[-1]), 1,
-                             ctypes.c_void_p(out2.data_ptr() + 16 * len(observables)), stream), "trace_prod")
+                             ctypes.c_void_p(out2.data_ptr() + 16 * nobs), stream), "trace_prod")
+    eye = torch.eye(2, dtype=dt, device=dev)
+    # [index, next site, last site, environment, operators]
+    active = []
     for k, obs in enumerate(observables):
         sites = sorted(obs)
-        lo, hi = sites[0], sites[-1]
-        E = Lenv[lo].unsqueeze(0)
-        for i in range(lo, hi + 1):
-            op = obs.get(i)
-            if op is None:
-                E = _norm_step(E[0], tensors[i]).unsqueeze(0)
+        ops_dev = {i: obs[i].to(device=dev, dtype=dt) for i in sites}
+        active.append([k, sites[0], sites[-1], Lenv[sites[0]], ops_dev])
+    while active:
+        groups = {}
+        for it in active:
+            groups.setdefault(tuple(tensors[it[1]].shape), []).append(it)
+        for (chiA, _, chiB), its in groups.items():
+            G = len(its)
+            E = torch.stack([it[3] for it in its])                               # [G, chiA, chiA]
+            A = torch.stack([tensors[it[1]] for it in its])                      # [G, chiA, 2, chiB]
+            W = torch.stack([it[4].get(it[1], eye) for it in its]).contiguous()  # [G, 2, 2]
+            M = _gemm(E, A.view(G, chiA, 2 * chiB))                              # [G, chiA, (s, chiB)]
+            X = torch.empty_like(M)
+            check(lib.agb_site_mix(code, ptr(M), ptr(W), ptr(X), G, chiA, chiB, stream), "site_mix")
+            En = _gemm(A.view(G, 2 * chiA, chiB), X.view(G, 2 * chiA, chiB), opA="C")  # [G, chiB, chiB]
+            for g, it in enumerate(its):
+                it[3] = En[g]
+                it[1] += 1
+        still = []
+        for it in active:
+            if it[1] > it[2]:
+                check(lib.agb_trace_prod(code, ptr(it[3]), ptr(Renv[it[2] + 1]), it[3].shape[0],
+                                         ctypes.c_void_p(out2.data_ptr() + 16 * it[0]), stream), "trace_prod")
             else:
-                W = op.to(device=dev, dtype=dt).reshape(1, 2, 2, 1)
-                E = _site_step(E, tensors[i], W)
-        check(lib.agb_trace_prod(code, ptr(E[0].contiguous()), ptr(Renv[hi + 1]), E.shape[1],
-                                 ctypes.c_void_p(out2.data_ptr() + 16 * k), stream), "trace_prod")
+                still.append(it)
+        active = still
     host = out2.cpu()
+    ops.check_tc_status(dev)
     norm = complex(host[-1, 0].item(), host[-1, 1].item())
-    return [complex(host[k, 0].item(), host[k, 1].item()) / norm for k in range(len(observables))]
+    return [complex(host[k, 0].item(), host[k, 1].item()) / norm for k in range(nobs)]

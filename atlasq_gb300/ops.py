@@ -117,8 +117,33 @@ def single_qubit_gate_(T, U):
     return T
 
 
-def cgemm_tc(A, B, opA="N", opB="N", alpha=1.0, beta=0.0, C=None):
-    """complex64 GEMM on the tcgen05 tensor cores (3xTF32); same contract as cgemm."""
+_TC_STATUS = {}
+
+
+def _tc_status_word(device):
+    dev = torch.device(device)
+    key = dev.index or 0
+    w = _TC_STATUS.get(key)
+    if w is None:
+        w = torch.zeros(1, dtype=torch.int32, device=dev)
+        _TC_STATUS[key] = w
+    return w
+
+
+def check_tc_status(device):
+    """Raise if a tensor-core GEMM issued with sync=False on `device` had a
+    bounded wait expire since the last check (reads one device word)."""
+    w = _tc_status_word(device)
+    v = int(w.item())
+    if v:
+        w.zero_()
+        check(v, "cgemm_tc")
+
+
+def cgemm_tc(A, B, opA="N", opB="N", alpha=1.0, beta=0.0, C=None, sync=True):
+    """complex64 GEMM on the tcgen05 tensor cores (3xTF32); same contract as cgemm.
+    sync=False issues it without synchronising the stream; check_tc_status()
+    reports a timeout of any such call."""
     lib = _lib.load()
     A, B = _c(A), _c(B)
     if A.dtype != torch.complex64:
@@ -139,9 +164,15 @@ def cgemm_tc(A, B, opA="N", opB="N", alpha=1.0, beta=0.0, C=None):
         C = C if batched else C.unsqueeze(0)
     need = lib.agb_cgemm_tc_workspace(bat, M, N, K)
     ws = workspace(need, A.device, "gemm_tc")
-    st = ctypes.c_int(0)
     al, be = complex(alpha), complex(beta)
-    check(lib.agb_cgemm_tc(opA.encode(), opB.encode(), bat, M, N, K, ptr(A2), ca, ra * ca, ptr(B2), cb, rb * cb,
-                           ptr(C), N, M * N, al.real, al.imag, be.real, be.imag, ptr(ws), ws.numel(),
-                           ctypes.byref(st), stream_ptr(A.device)), "cgemm_tc")
+    if sync:
+        st = ctypes.c_int(0)
+        check(lib.agb_cgemm_tc(opA.encode(), opB.encode(), bat, M, N, K, ptr(A2), ca, ra * ca, ptr(B2), cb,
+                               rb * cb, ptr(C), N, M * N, al.real, al.imag, be.real, be.imag, ptr(ws), ws.numel(),
+                               ctypes.byref(st), stream_ptr(A.device)), "cgemm_tc")
+    else:
+        check(lib.agb_cgemm_tc_async(opA.encode(), opB.encode(), bat, M, N, K, ptr(A2), ca, ra * ca, ptr(B2), cb,
+                                     rb * cb, ptr(C), N, M * N, al.real, al.imag, be.real, be.imag, ptr(ws),
+                                     ws.numel(), ptr(_tc_status_word(A.device)), stream_ptr(A.device)),
+              "cgemm_tc")
     return C if batched else C[0]

@@ -42,7 +42,7 @@ def sample_tensors(tensors, num_shots, seed, chunk=16384, return_pz=False):
             l, _, r = T.shape
             Tm = T.reshape(l, 2 * r)
             use_tc = dt == torch.complex64 and ns >= 64 and 2 * r >= 64 and l >= 32
-            temp = ops.cgemm_tc(L, Tm) if use_tc else ops.cgemm(L, Tm)
+            temp = ops.cgemm_tc(L, Tm, sync=False) if use_tc else ops.cgemm(L, Tm)
             Lnew = torch.empty(ns, r, dtype=dt, device=dev) if i < n - 1 else None
             check(lib.agb_sample_site(code, ptr(temp), ns, r, i, ctypes.c_uint64(seed & 0xFFFFFFFFFFFFFFFF),
                                       ctypes.c_uint64(c0), ctypes.c_void_p(bits.data_ptr() + 8 * c0),
@@ -51,6 +51,8 @@ def sample_tensors(tensors, num_shots, seed, chunk=16384, return_pz=False):
             if return_pz:
                 pz[c0:c0 + ns, i] = pzcol[:ns]
             L = Lnew
+    if dt == torch.complex64:
+        ops.check_tc_status(dev)
     return (bits, pz) if return_pz else bits
 
 

@@ -186,7 +186,13 @@ int agb_sample_site(int dtype, const void* temp, int shots, int chiR, int site, 
  * N[R][a][t][B] = sum_{L,s} W[L][s][t][R] M[L][a][s][B]. */
 int agb_mpo_mix(int dtype, const void* M, const void* W, void* N, int Lw, int Rw, int chiA, int chiB,
                 void* stream);
-/* out2[0] + i out2[1] = sum_{r,c} E[r,c] Q[c,r]  (double accumulation; out2 is device memory). */
+/* (a10) The single-site form of the same mixing for a batch of `count` items, one
+ * 2x2 operator each (W: count x 2 x 2, contiguous):
+ * N[g][a][t][b] = sum_s W[g][s][t] M[g][a][s][b], M and N count x chiA x 2 x chiB.
+ * The per-site einsum of expectation_value with a [1,2,2,1] MPO tensor
+ * (src/atlas_q/mpo_ops.py:1145), batched over the observables of a sweep. */
+int agb_site_mix(int dtype, const void* M, const void* W, void* N, int count, int chiA, int chiB, void* stream);
+/* out2[0] + i out2[1] = sum_{r,c} E[r,c] Q[c,r]  (double accuracy; out2 is device memory). */
 int agb_trace_prod(int dtype, const void* E, const void* Q, int n, double* out2, void* stream);
 
 /* Per-stage CUDA-event timer of the two-site pipeline (this build's own
@@ -228,6 +234,13 @@ int agb_cgemm_tc(char opA, char opB, int batch, int M, int N, int K, const void*
                  int64_t strideA, const void* B, int64_t ldb, int64_t strideB, void* C, int64_t ldc,
                  int64_t strideC, float alpha_re, float alpha_im, float beta_re, float beta_im, void* ws,
                  size_t ws_bytes, int* status_host, void* stream);
+/* The same GEMM without any synchronisation: a bounded wait that expires sets
+ * *status_dev (device memory) to AGB_ERR_TIMEOUT; the word is never cleared
+ * by the library, so one read after a sequence of calls checks them all. */
+int agb_cgemm_tc_async(char opA, char opB, int batch, int M, int N, int K, const void* A, int64_t lda,
+                       int64_t strideA, const void* B, int64_t ldb, int64_t strideB, void* C, int64_t ldc,
+                       int64_t strideC, float alpha_re, float alpha_im, float beta_re, float beta_im, void* ws,
+                       size_t ws_bytes, int* status_dev, void* stream);
 
 /* Batched complex GEMM (SIMT reference-free kernel, used by the host layer):
  * C[b] = alpha * op(A[b]) op(B[b]) + beta * C[b]; op: 'N','T','C'. */
