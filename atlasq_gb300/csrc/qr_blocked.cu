@@ -40,7 +40,7 @@ template <> struct QrbCfg<double2> { static constexpr int QB = 8; };
 
 struct QrbLayout {
   int QB, C, P, PF, npo, ld;
-  size_t panels, vloc, w, w2, t, total;  // byte offsets
+  size_t panels, vloc, w, w2, t, vb, total;  // byte offsets
 };
 
 AGB_HD QrbLayout qrb_layout(int esz, int QB, int M, int N, int C) {
@@ -58,6 +58,7 @@ AGB_HD QrbLayout qrb_layout(int esz, int QB, int M, int N, int C) {
   L.w = o;      o += (size_t)QB * L.npo * QB * esz;
   L.w2 = o;     o += (size_t)QB * L.npo * QB * esz;
   L.t = o;      o += (size_t)QB * QB * esz;
+  L.vb = o;     o += (size_t)2 * M * esz;
   L.total = o;
   return L;
 }
@@ -170,7 +171,7 @@ AGB_DEV void qrb_apply(CX* Y, const int* ycols, int ncol, const CX* V, const CX*
   __syncthreads();
 }
 
-template <typename CX>
+template <typename CX, int NK>
 __global__ void __launch_bounds__(QBT, 1)
     qr_blocked_kernel(const CX* __restrict__ Ain, int M, int N, int transA, CX* Q, CX* R, int trans_out, CX* Vg,
                       CX* Tg, int C) {
@@ -188,6 +189,7 @@ __global__ void __launch_bounds__(QBT, 1)
   CX* W = (CX*)(smem_raw + Lo.w);
   CX* W2 = (CX*)(smem_raw + Lo.w2);
   CX* Tl = (CX*)(smem_raw + Lo.t);
+  CX* vbuf = (CX*)(smem_raw + Lo.vb);  // [2][M] the current reflector, double-buffered
   __shared__ int ycols[kQrbMaxCols];
   __shared__ int ycount;
   __shared__ CX taus[QB];
@@ -214,44 +216,92 @@ __global__ void __launch_bounds__(QBT, 1)
       CX* P0 = pan + (size_t)(s * QB) * ld;
       const int pw = min(QB, N - pb);  // columns in the panel
       const int bw = min(QB, kk - pb);  // columns factored
+      // The panel in registers: warp w holds column w, lane `lane` its rows
+      // lane + 32 k.  Per column the owner warp forms the reflector and writes
+      // v to a shared vector (double-buffered by column parity: the next
+      // owner cannot overwrite it before every warp has passed the barrier of
+      // the column in between); one block barrier; the later warps apply it.
+      CX x[NK];
+      if (wid < pw) {
+        const CX* col = P0 + (size_t)wid * ld;
+#pragma unroll
+        for (int k = 0; k < NK; ++k) {
+          const int r = lane + 32 * k;
+          x[k] = (r < M) ? col[r] : czero<CX>();
+        }
+      }
       for (int jj = 0; jj < bw; ++jj) {
         const int c = pb + jj;
+        CX* vb = vbuf + (size_t)(jj & 1) * M;
         if (wid == jj) {
-          CX* col = P0 + (size_t)jj * ld;
           Rt part = 0;
-          for (int r = c + 1 + lane; r < M; r += 32) part += cabs2(col[r]);
-          const Rt xn2 = warp_sum(part);
-          CX t = czero<CX>(), sc = czero<CX>();
-          if (lane == 0) {
-            const CX alpha = col[c];
-            Rt beta;
-            if (xn2 == Rt(0) && alpha.y == Rt(0)) {
-              beta = alpha.x;
-            } else {
-              beta = -copysign(sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xn2), alpha.x);
-              t = mk<CX>((beta - alpha.x) / beta, -alpha.y / beta);
-              sc = cinv(csub(alpha, mk<CX>(beta, 0)));
-            }
-            col[c] = mk<CX>(beta, 0);
-            taus[jj] = t;
+          CX am = czero<CX>();
+#pragma unroll
+          for (int k = 0; k < NK; ++k) {
+            const int r = lane + 32 * k;
+            if (r > c && r < M) part += cabs2(x[k]);
+            if (r == c) am = x[k];
           }
-          sc.x = __shfl_sync(0xffffffffu, sc.x, 0);
-          sc.y = __shfl_sync(0xffffffffu, sc.y, 0);
-          for (int r = c + 1 + lane; r < M; r += 32) col[r] = cmul(col[r], sc);  // v below the diagonal
+          const Rt xn2 = warp_sum(part);
+          CX alpha;
+          alpha.x = __shfl_sync(0xffffffffu, am.x, c & 31);
+          alpha.y = __shfl_sync(0xffffffffu, am.y, c & 31);
+          CX t = czero<CX>(), sc = czero<CX>();
+          Rt beta;
+          if (xn2 == Rt(0) && alpha.y == Rt(0)) {
+            beta = alpha.x;
+          } else {
+            beta = -copysign(sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xn2), alpha.x);
+            t = mk<CX>((beta - alpha.x) / beta, -alpha.y / beta);
+            sc = cinv(csub(alpha, mk<CX>(beta, 0)));
+          }
+#pragma unroll
+          for (int k = 0; k < NK; ++k) {
+            const int r = lane + 32 * k;
+            if (r < M) {
+              CX v = czero<CX>();
+              if (r == c) {
+                v = mk<CX>(1, 0);
+                x[k] = mk<CX>(beta, 0);
+              } else if (r > c) {
+                x[k] = cmul(x[k], sc);  // v below the diagonal
+                v = x[k];
+              }
+              vb[r] = v;
+            }
+          }
+          if (lane == 0) taus[jj] = t;
         }
         __syncthreads();
-        // H_c^H = I - conj(tau) v v^H on the panel's later columns (warp per column)
+        // H_c^H = I - conj(tau) v v^H on the panel's later columns
         if (wid > jj && wid < pw) {
           const CX t = taus[jj];
           if (t.x != Rt(0) || t.y != Rt(0)) {
-            const CX* v = P0 + (size_t)jj * ld;
-            CX* col = P0 + (size_t)wid * ld;
-            CX acc = czero<CX>();
-            for (int r = c + lane; r < M; r += 32) cfmac(acc, (r == c) ? mk<CX>(1, 0) : v[r], col[r]);
-            acc = warp_csum(acc);
+            CX a0 = czero<CX>(), a1 = czero<CX>();
+#pragma unroll
+            for (int k = 0; k < NK; ++k) {
+              const int r = lane + 32 * k;
+              if (r >= c && r < M) {
+                if (k & 1) cfmac(a1, vb[r], x[k]);
+                else cfmac(a0, vb[r], x[k]);
+              }
+            }
+            const CX acc = warp_csum(cadd(a0, a1));
             const CX tw = cmul(cconj(t), acc);
-            for (int r = c + lane; r < M; r += 32) col[r] = csub(col[r], cmul((r == c) ? mk<CX>(1, 0) : v[r], tw));
+#pragma unroll
+            for (int k = 0; k < NK; ++k) {
+              const int r = lane + 32 * k;
+              if (r >= c && r < M) x[k] = csub(x[k], cmul(vb[r], tw));
+            }
           }
+        }
+      }
+      if (wid < pw) {
+        CX* col = P0 + (size_t)wid * ld;
+#pragma unroll
+        for (int k = 0; k < NK; ++k) {
+          const int r = lane + 32 * k;
+          if (r < M) col[r] = x[k];
         }
       }
       __syncthreads();
@@ -279,22 +329,28 @@ __global__ void __launch_bounds__(QBT, 1)
         }
       }
       __syncthreads();
-      // T (forward, columnwise): T[i][i] = tau_i, T[0:i][i] = -tau_i T[0:i][0:i] S[0:i][i]
+      // T (forward, columnwise): T[i][i] = tau_i, T[0:i][i] = -tau_i T[0:i][0:i] S[0:i][i];
+      // lane k of warp 0 holds row k of T in registers
       if (wid == 0) {
-        CX* Tp = Tg + (size_t)p * QB * QB;
-        for (int e = lane; e < QB * QB; e += 32) Tl[e] = czero<CX>();
-        __syncwarp();
-        for (int i = 0; i < bw; ++i) {
-          const CX ti = taus[i];
-          CX acc = czero<CX>();
-          if (lane < i)
-            for (int m = lane; m < i; ++m) cfma(acc, Tl[lane * QB + m], Ssh[m * QB + i]);
-          __syncwarp();
-          if (lane < i) Tl[lane * QB + i] = cmul(mk<CX>(-ti.x, -ti.y), acc);
-          if (lane == 0) Tl[i * QB + i] = ti;
-          __syncwarp();
+        CX trow[QB];
+#pragma unroll
+        for (int m = 0; m < QB; ++m) trow[m] = czero<CX>();
+#pragma unroll
+        for (int i = 0; i < QB; ++i) {
+          if (i < bw) {
+            const CX ti = taus[i];
+            CX acc = czero<CX>();
+#pragma unroll
+            for (int m = 0; m < i; ++m)
+              if (m >= lane) cfma(acc, trow[m], Ssh[m * QB + i]);
+            if (lane < i) trow[i] = cmul(mk<CX>(-ti.x, -ti.y), acc);
+            else if (lane == i) trow[i] = ti;
+          }
         }
-        for (int e = lane; e < QB * QB; e += 32) Tp[e] = Tl[e];
+        CX* Tp = Tg + (size_t)p * QB * QB;
+        if (lane < QB)
+#pragma unroll
+          for (int m = 0; m < QB; ++m) Tp[lane * QB + m] = trow[m];
       }
       __threadfence();  // V_p, T_p visible to the cluster before the barrier
     }
@@ -391,10 +447,28 @@ __global__ void __launch_bounds__(QBT, 1)
   cluster.sync();
 }
 
+template <typename CX>
+using QrbKernel = void (*)(const CX*, int, int, int, CX*, CX*, int, CX*, CX*, int);
+
+// The instance whose per-lane register column (NK rows per lane) covers M rows;
+// nullptr above 1024 rows (512 for complex128, whose columns would spill).
+template <typename CX>
+QrbKernel<CX> qrb_kernel_for(int M) {
+  if (M <= 128) return qr_blocked_kernel<CX, 4>;
+  if (M <= 256) return qr_blocked_kernel<CX, 8>;
+  if (M <= 512) return qr_blocked_kernel<CX, 16>;
+  if constexpr (sizeof(CX) == 8) {
+    if (M <= 1024) return qr_blocked_kernel<CX, 32>;
+  }
+  return nullptr;
+}
+
 // Cluster size for the blocked kernel: the largest of 16, 8, 4, 2 CTAs not
 // above the panel count whose shared memory fits; 0 if none.
 template <typename CX>
 int qrb_cluster_size(int M, int N, size_t* smem_out) {
+  const QrbKernel<CX> kern = qrb_kernel_for<CX>(M);
+  if (!kern) return 0;
   constexpr int QB = QrbCfg<CX>::QB;
   const int P = (N + QB - 1) / QB;
   static int allow16 = -1;
@@ -405,9 +479,9 @@ int qrb_cluster_size(int M, int N, size_t* smem_out) {
     if (C == 16) {
       if (allow16 < 0) {
         allow16 = 0;
-        if (cudaFuncSetAttribute(qr_blocked_kernel<CX>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+        if (cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
                 cudaSuccess &&
-            cudaFuncSetAttribute(qr_blocked_kernel<CX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)kQrbSmemBudget) == cudaSuccess) {
           cudaLaunchConfig_t cfg = {};
           cfg.gridDim = dim3(16, 1, 1);
@@ -421,7 +495,7 @@ int qrb_cluster_size(int M, int N, size_t* smem_out) {
           cfg.attrs = attr;
           cfg.numAttrs = 1;
           int ncl = 0;
-          if (cudaOccupancyMaxActiveClusters(&ncl, qr_blocked_kernel<CX>, &cfg) == cudaSuccess && ncl > 0)
+          if (cudaOccupancyMaxActiveClusters(&ncl, kern, &cfg) == cudaSuccess && ncl > 0)
             allow16 = 1;
         }
         cudaGetLastError();
@@ -451,13 +525,12 @@ int launch_qr_blocked(const CX* A, int M, int N, int transA, CX* Q, CX* R, int t
   size_t smem = 0;
   const int C = qrb_cluster_size<CX>(M, N, &smem);
   if (C == 0) return AGB_ERR_UNSUPPORTED;
-  if (C > 8 && cudaFuncSetAttribute(qr_blocked_kernel<CX>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
-                   cudaSuccess) {
+  const QrbKernel<CX> kern = qrb_kernel_for<CX>(M);
+  if (C > 8 && cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
     cudaGetLastError();
     return AGB_ERR_UNSUPPORTED;
   }
-  if (cudaFuncSetAttribute(qr_blocked_kernel<CX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-      cudaSuccess) {
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
     cudaGetLastError();
     return AGB_ERR_UNSUPPORTED;
   }
@@ -478,7 +551,7 @@ int launch_qr_blocked(const CX* A, int M, int N, int transA, CX* Q, CX* R, int t
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  const cudaError_t err = cudaLaunchKernelEx(&cfg, qr_blocked_kernel<CX>, A, M, N, transA, Q, R, trans_out, Vg, Tg, C);
+  const cudaError_t err = cudaLaunchKernelEx(&cfg, kern, A, M, N, transA, Q, R, trans_out, Vg, Tg, C);
   agb_note_launch();
   if (err != cudaSuccess) {
     cudaGetLastError();
