@@ -886,9 +886,13 @@ __global__ void polish_setup_kernel(const HeevdProb* __restrict__ probs, GemmPro
   gp[count + i] = h;
 }
 
-// V = Q Y with the reflector of each step staged once per CTA in shared memory
-// (double-buffered, one barrier per reflector); each warp owns two columns of Y
-// held in registers.  WARPS warps per CTA -> 2*WARPS columns per CTA.
+// V = Q Y, reflectors applied in pairs (j, j-1), each pair staged once per CTA
+// in shared memory (double-buffered, one barrier per pair); each warp owns two
+// columns of Y held in registers.  WARPS warps per CTA -> 2*WARPS columns.
+//   H_{j-1} H_j z = z - v_j s1 - v_{j-1} s2 with
+//   s1 = tau_j (v_j^H z),  s2 = tau_{j-1} (v_{j-1}^H z - (v_{j-1}^H v_j) s1):
+// one pass forms the three dot products (the last one does not depend on z),
+// one pass applies both reflectors.
 template <typename CX, int NK, int WARPS>
 __global__ void __launch_bounds__(WARPS * 32) backtransform2_kernel(const HeevdProb* __restrict__ probs) {
   typedef typename cx_traits<CX>::R R;
@@ -896,7 +900,8 @@ __global__ void __launch_bounds__(WARPS * 32) backtransform2_kernel(const HeevdP
   const int n = P.n, ell = P.ell, nv = P.nvec;
   const int col0 = blockIdx.x * 2 * WARPS;
   if (col0 >= nv || n > NK * 32 || P.skip_vectors) return;
-  __shared__ CX vbuf[2][NK * 32];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  CX* vbuf = (CX*)smem_raw;  // [2 buffers][2 reflectors][NK * 32]
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const int t0 = col0 + 2 * wid, t1 = t0 + 1;
   const bool h0 = t0 < nv, h1 = t1 < nv;
@@ -910,54 +915,70 @@ __global__ void __launch_bounds__(WARPS * 32) backtransform2_kernel(const HeevdP
   }
   const CX* H = (const CX*)P.H;
   const CX* tau = (const CX*)P.tau;
-  // reflector j is read from global memory one step ahead (registers), so the
-  // L2 round trip overlaps the previous reflector's work instead of preceding
-  // every barrier; thread tid stages rows tid + WARPS * 32 * u
+  // the rows of the next pair are read from global memory one pair ahead
+  // (registers), so the L2 round trip overlaps the current pair's work;
+  // thread tid stages rows tid + WARPS * 32 * u
   constexpr int PF = (NK * 32 + WARPS * 32 - 1) / (WARPS * 32);
-  CX pf[PF];
-  CX tnext = czero<CX>();
-  auto fetch = [&](int j) {
+  CX pa[PF], pb[PF];
+  CX ta = czero<CX>(), tb = czero<CX>();
+  auto fetch = [&](int j) {  // reflectors j and j-1 (if j >= 1)
     const CX* row = H + (int64_t)j * P.ldh;
+    const CX* row2 = H + (int64_t)(j - 1) * P.ldh;
 #pragma unroll
     for (int u = 0; u < PF; ++u) {
       const int r = tid + WARPS * 32 * u;
-      pf[u] = (r < n && r > j + 1) ? row[r] : czero<CX>();
+      pa[u] = (r < n && r > j + 1) ? row[r] : czero<CX>();
+      pb[u] = (j >= 1 && r < n && r > j) ? row2[r] : czero<CX>();
     }
-    tnext = tau[j];
+    ta = tau[j];
+    tb = (j >= 1) ? tau[j - 1] : czero<CX>();
   };
   if (n >= 2) fetch(n - 2);
-  for (int j = n - 2; j >= 0; --j) {
-    CX* buf = vbuf[j & 1];
+  for (int j = n - 2; j >= 0; j -= 2) {
+    CX* b1 = vbuf + (size_t)((j >> 1) & 1) * 2 * (NK * 32);  // v_j
+    CX* b2 = b1 + NK * 32;                                    // v_{j-1} (zero when j == 0)
 #pragma unroll
     for (int u = 0; u < PF; ++u) {
       const int r = tid + WARPS * 32 * u;
-      if (r < n) buf[r] = (r == j + 1) ? mk<CX>(1, 0) : pf[u];
-    }
-    const CX tj = tnext;
-    if (j >= 1) fetch(j - 1);
-    __syncthreads();
-    if (tj.x == R(0) && tj.y == R(0)) continue;
-    CX s0 = czero<CX>(), s1 = czero<CX>();
-    // v_j is zero in rows <= j: chunks of 32 rows below that are skipped
-    // (a warp-uniform test, so the register arrays keep static indices)
-#pragma unroll
-    for (int k = 0; k < NK; ++k) {
-      const int r = lane + 32 * k;
-      if (32 * k + 31 > j && r < n) {
-        const CX vr = buf[r];
-        cfmac(s0, vr, z0[k]);
-        cfmac(s1, vr, z1[k]);
+      if (r < n) {
+        b1[r] = (r == j + 1) ? mk<CX>(1, 0) : pa[u];
+        b2[r] = (j >= 1 && r == j) ? mk<CX>(1, 0) : pb[u];
       }
     }
-    s0 = cmul(tj, warp_csum(s0));
-    s1 = cmul(tj, warp_csum(s1));
+    const CX t1 = ta, t2 = tb;
+    if (j >= 2) fetch(j - 2);
+    __syncthreads();
+    const bool a1 = (t1.x != R(0) || t1.y != R(0)), a2 = (t2.x != R(0) || t2.y != R(0));
+    if (!a1 && !a2) continue;
+    CX d10 = czero<CX>(), d11 = czero<CX>(), d20 = czero<CX>(), d21 = czero<CX>(), c = czero<CX>();
+    // v_j and v_{j-1} are zero in rows < j: chunks of 32 rows below that are
+    // skipped (a warp-uniform test, so the register arrays keep static indices)
 #pragma unroll
     for (int k = 0; k < NK; ++k) {
       const int r = lane + 32 * k;
-      if (32 * k + 31 > j && r < n) {
-        const CX vr = buf[r];
-        z0[k] = csub(z0[k], cmul(vr, s0));
-        z1[k] = csub(z1[k], cmul(vr, s1));
+      if (32 * k + 31 >= j && r < n) {
+        const CX v1 = b1[r], v2 = b2[r];
+        cfmac(d10, v1, z0[k]);
+        cfmac(d11, v1, z1[k]);
+        cfmac(d20, v2, z0[k]);
+        cfmac(d21, v2, z1[k]);
+        cfmac(c, v2, v1);
+      }
+    }
+    d10 = warp_csum(d10);
+    d11 = warp_csum(d11);
+    d20 = warp_csum(d20);
+    d21 = warp_csum(d21);
+    c = warp_csum(c);
+    const CX s10 = cmul(t1, d10), s11 = cmul(t1, d11);
+    const CX s20 = cmul(t2, csub(d20, cmul(c, s10))), s21 = cmul(t2, csub(d21, cmul(c, s11)));
+#pragma unroll
+    for (int k = 0; k < NK; ++k) {
+      const int r = lane + 32 * k;
+      if (32 * k + 31 >= j && r < n) {
+        const CX v1 = b1[r], v2 = b2[r];
+        z0[k] = csub(z0[k], cadd(cmul(v1, s10), cmul(v2, s20)));
+        z1[k] = csub(z1[k], cadd(cmul(v1, s11), cmul(v2, s21)));
       }
     }
   }
@@ -975,8 +996,18 @@ __global__ void __launch_bounds__(WARPS * 32) backtransform2_kernel(const HeevdP
 template <typename CX, int NK>
 int launch_bt(const HeevdProb* probs, int count, int maxell, cudaStream_t s) {
   constexpr int WARPS = (sizeof(CX) * NK > 128) ? 8 : 16;
+  constexpr size_t smem = (size_t)4 * NK * 32 * sizeof(CX);
+  if (smem > 48 * 1024) {
+    static bool set = false;
+    if (!set) {
+      if (cudaFuncSetAttribute(backtransform2_kernel<CX, NK, WARPS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem) != cudaSuccess)
+        return AGB_ERR_CUDA;
+      set = true;
+    }
+  }
   dim3 grid((maxell + 2 * WARPS - 1) / (2 * WARPS), count);
-  backtransform2_kernel<CX, NK, WARPS><<<grid, WARPS * 32, 0, s>>>(probs);
+  backtransform2_kernel<CX, NK, WARPS><<<grid, WARPS * 32, smem, s>>>(probs);
   AGB_CHECK_LAUNCH();
   return AGB_OK;
 }
