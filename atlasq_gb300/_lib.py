@@ -79,6 +79,7 @@ _SIGS = {
     "agb_site_mix": (I, [I, P, P, P, I, I, I, P]),
     "agb_prof_begin": (I, [I]),
     "agb_launch_count": (ctypes.c_longlong, []),
+    "agb_last_error": (ctypes.c_char_p, []),
     "agb_prof_end": (I, [P, P, I]),
     "agb_mlp_forward": (I, [P, P, I, P, P]),
     "agb_mlp_backward": (I, [P, P, P, I, P, P, P]),
@@ -120,7 +121,12 @@ def load(build_if_missing=True):
 def check(rc, what=""):
     if rc != AGB_OK:
         exc, msg = _ERRS.get(rc, (RuntimeError, f"error {rc}"))
-        raise exc(f"atlasq_gb300: {what}: {msg} (status {rc})")
+        where = ""
+        if rc == AGB_ERR_CUDA and _lib is not None:
+            site = _lib.agb_last_error()
+            if site:
+                where = f" at {site.decode(errors='replace')}"
+        raise exc(f"atlasq_gb300: {what}: {msg} (status {rc}){where}")
 
 
 def require_cuda(device):

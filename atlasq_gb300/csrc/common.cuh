@@ -190,12 +190,29 @@ AGB_DEV float philox_normal(uint64_t seed, uint64_t idx, uint32_t stream) {
 
 AGB_HD size_t agb_align(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// Opts `kern` in to `dyn` bytes of dynamic shared memory when its static plus
+// dynamic shared memory exceeds the 48 KiB a launch gets by default (a launch
+// over that limit without the opt-in is refused with cudaErrorInvalidValue).
+template <typename K>
+inline cudaError_t agb_smem_optin(K kern, size_t dyn) {
+  cudaFuncAttributes a;
+  cudaError_t e = cudaFuncGetAttributes(&a, kern);
+  if (e != cudaSuccess) return e;
+  if (a.sharedSizeBytes + dyn <= 48 * 1024) return cudaSuccess;
+  return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+}
+
 // Counts kernel launches issued by this library (read with agb_launch_count).
 void agb_note_launch();
+// Records where a launch check failed (read with agb_last_error).
+void agb_note_error(const char* file, int line, cudaError_t e);
 
 #define AGB_CHECK_LAUNCH()                      \
   do {                                          \
     agb_note_launch();                          \
     cudaError_t _e = cudaGetLastError();        \
-    if (_e != cudaSuccess) return AGB_ERR_CUDA; \
+    if (_e != cudaSuccess) {                    \
+      agb_note_error(__FILE__, __LINE__, _e);   \
+      return AGB_ERR_CUDA;                      \
+    }                                           \
   } while (0)

@@ -997,14 +997,10 @@ template <typename CX, int NK>
 int launch_bt(const HeevdProb* probs, int count, int maxell, cudaStream_t s) {
   constexpr int WARPS = (sizeof(CX) * NK > 128) ? 8 : 16;
   constexpr size_t smem = (size_t)4 * NK * 32 * sizeof(CX);
-  if (smem > 48 * 1024) {
-    static bool set = false;
-    if (!set) {
-      if (cudaFuncSetAttribute(backtransform2_kernel<CX, NK, WARPS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)smem) != cudaSuccess)
-        return AGB_ERR_CUDA;
-      set = true;
-    }
+  const cudaError_t oe = agb_smem_optin(backtransform2_kernel<CX, NK, WARPS>, smem);
+  if (oe != cudaSuccess) {
+    agb_note_error(__FILE__, __LINE__, oe);
+    return AGB_ERR_CUDA;
   }
   dim3 grid((maxell + 2 * WARPS - 1) / (2 * WARPS), count);
   backtransform2_kernel<CX, NK, WARPS><<<grid, WARPS * 32, smem, s>>>(probs);
@@ -1062,8 +1058,11 @@ int launch_heevd_vectors(HeevdProb* probs, GemmProb* gp, int count, int maxn, in
     int zcap = base < budget ? (int)((budget - base) / ((size_t)maxn * sizeof(R))) : 0;
     if (zcap > maxell) zcap = maxell;
     const size_t sm = base + (size_t)zcap * maxn * sizeof(R);
-    if (sm > 48 * 1024)
-      cudaFuncSetAttribute(cluster_invit_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    const cudaError_t oe = agb_smem_optin(cluster_invit_kernel<R>, sm);
+    if (oe != cudaSuccess) {
+      agb_note_error(__FILE__, __LINE__, oe);
+      return AGB_ERR_CUDA;
+    }
     const int maxcl = maxell / 2 > 0 ? maxell / 2 : 1;
     cluster_list_kernel<R><<<(count + 127) / 128, 128, 0, s>>>(probs, count, kClusterTolRel);
     AGB_CHECK_LAUNCH();

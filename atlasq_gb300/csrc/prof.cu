@@ -1,3 +1,4 @@
+#include <stdio.h>
 // Per-stage CUDA-event timing of the two-site pipeline.  When enabled, each
 // stage boundary records an event on the launching stream; agb_prof_end sums
 // the elapsed time between consecutive marks per stage.  Events are created
@@ -20,6 +21,19 @@ long long g_launches = 0;
 void agb_note_launch() { ++g_launches; }
 
 extern "C" long long agb_launch_count(void) { return g_launches; }
+
+// The most recent failed launch check: "file:line: cudaErrorName (description)".
+static char g_last_error[256] = "";
+
+void agb_note_error(const char* file, int line, cudaError_t e) {
+  const char* base = file;
+  for (const char* p = file; *p; ++p)
+    if (*p == '/') base = p + 1;
+  snprintf(g_last_error, sizeof(g_last_error), "%s:%d: %s (%s)", base, line, cudaGetErrorName(e),
+           cudaGetErrorString(e));
+}
+
+extern "C" const char* agb_last_error(void) { return g_last_error; }
 
 void prof_mark(int stage, cudaStream_t s) {
   if (!g_prof.on) return;

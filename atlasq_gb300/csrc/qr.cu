@@ -191,11 +191,11 @@ extern "C" int agb_qr(int dtype, const void* A, int M, int N, int transA, void* 
     if (rc == AGB_OK) return AGB_OK;
   }
   if (dtype == AGB_C64) {
-    if (smem > 48 * 1024) cudaFuncSetAttribute(qr_kernel<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (agb_smem_optin(qr_kernel<float2>, smem) != cudaSuccess) return AGB_ERR_CUDA;
     qr_kernel<float2><<<1, 1024, smem, s>>>((const float2*)A, M, N, transA, (float2*)W, (float2*)Q,
                                              (float2*)R, trans_out, (float2*)tau, (float2*)Qw);
   } else {
-    if (smem > 48 * 1024) cudaFuncSetAttribute(qr_kernel<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (agb_smem_optin(qr_kernel<double2>, smem) != cudaSuccess) return AGB_ERR_CUDA;
     qr_kernel<double2><<<1, 1024, smem, s>>>((const double2*)A, M, N, transA, (double2*)W,
                                               (double2*)Q, (double2*)R, trans_out, (double2*)tau, (double2*)Qw);
   }
@@ -265,11 +265,11 @@ extern "C" int agb_qr_noalloc(int dtype, const void* A, int M, int N, int transA
   const size_t smem = (size_t)M * esz + (size_t)QR_RG * QR_CG * esz;
   cudaStream_t s = (cudaStream_t)stream;
   if (dtype == AGB_C64) {
-    if (smem > 48 * 1024) cudaFuncSetAttribute(qr_kernel<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (agb_smem_optin(qr_kernel<float2>, smem) != cudaSuccess) return AGB_ERR_CUDA;
     qr_kernel<float2><<<1, 1024, smem, s>>>((const float2*)A, M, N, transA, (float2*)W, (float2*)Q,
                                              (float2*)R, trans_out, (float2*)tau, (float2*)Qw);
   } else {
-    if (smem > 48 * 1024) cudaFuncSetAttribute(qr_kernel<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (agb_smem_optin(qr_kernel<double2>, smem) != cudaSuccess) return AGB_ERR_CUDA;
     qr_kernel<double2><<<1, 1024, smem, s>>>((const double2*)A, M, N, transA, (double2*)W,
                                               (double2*)Q, (double2*)R, trans_out, (double2*)tau, (double2*)Qw);
   }

@@ -360,7 +360,10 @@ int launch_tridiag_cluster_C(const HeevdProb* probs, int count, int maxn, int C,
   cfg.numAttrs = 1;
   cudaError_t err = cudaLaunchKernelEx(&cfg, kern, probs, C, cap_elems);
   agb_note_launch();
-  if (err != cudaSuccess) return AGB_ERR_CUDA;
+  if (err != cudaSuccess) {
+    agb_note_error(__FILE__, __LINE__, err);
+    return AGB_ERR_CUDA;
+  }
   return AGB_OK;
 }
 

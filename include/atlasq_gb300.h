@@ -195,6 +195,11 @@ int agb_site_mix(int dtype, const void* M, const void* W, void* N, int count, in
 /* out2[0] + i out2[1] = sum_{r,c} E[r,c] Q[c,r]  (double accuracy; out2 is device memory). */
 int agb_trace_prod(int dtype, const void* E, const void* Q, int n, double* out2, void* stream);
 
+/* Where the most recent failed launch check of this library was, as
+ * "file:line: cudaErrorName (description)"; empty if none (this build's own
+ * diagnostics; the string is owned by the library). */
+const char* agb_last_error(void);
+
 /* Per-stage CUDA-event timer of the two-site pipeline (this build's own
  * instrumentation; no reference counterpart).  agb_prof_begin enables marks on
  * the launching stream (capacity = max marks); agb_prof_end disables them and

@@ -110,6 +110,28 @@ def _hermitian_cases():
     return cases
 
 
+@pytest.mark.parametrize("n,ell", [(192, 50), (256, 35), (384, 24)])
+@pytest.mark.parametrize("dt", [torch.complex64, torch.complex128])
+def test_heevd_vector_phase_near_the_default_shared_memory_limit(n, ell, dt):
+    """Sizes whose cluster inverse-iteration launch takes just under 48 KiB of
+    dynamic shared memory: with the kernel's static shared memory the launch
+    needs the opt-in, which was once granted only above 48 KiB of dynamic
+    memory (the launch was refused with cudaErrorInvalidValue)."""
+    g = torch.Generator().manual_seed(n + ell)
+    Q, _ = torch.linalg.qr(crandn(n, n, gen=g, dtype=torch.complex128))
+    w = torch.linspace(1.0, 0.01, n, dtype=torch.float64).to(torch.complex128)
+    H = (Q * w) @ Q.conj().T
+    H = (H + H.conj().T) / 2
+    wv, V = ops.heevd(H.to(dt).to(DEV), ell=ell)
+    wv = wv.cpu().double().numpy()
+    V = V.cpu().to(torch.complex128).numpy()
+    Hn = H.numpy()
+    ref = np.linalg.eigvalsh(Hn)[::-1][:ell]
+    tol = 5e-5 if dt == torch.complex64 else 1e-11
+    assert np.max(np.abs(wv - ref)) <= tol
+    assert np.linalg.norm(Hn @ V - V * wv[None, :]) <= tol * np.sqrt(ell)
+
+
 @pytest.mark.parametrize("case", range(14))
 @pytest.mark.parametrize("dt", [torch.complex64, torch.complex128])
 def test_heevd_residual_and_orthonormality(case, dt):
