@@ -413,7 +413,7 @@ __global__ void __launch_bounds__(512) prerank_kernel(int64_t* __restrict__ desc
   if (nv >= ell) return;
   // do not split a cluster (the tolerance of the cluster kernel)
   const R scl = fmax(fabs(lam[0]), fabs(lam[ell - 1]));
-  const R tol = (R)kClusterTolRel * fmax(scl, (R)(sizeof(R) == 4 ? 1e-30 : 1e-290));
+  const R tol = (R)cluster_tol_rel(n) * fmax(scl, (R)(sizeof(R) == 4 ? 1e-30 : 1e-290));
   while (nv < ell && (lam[nv - 1] - lam[nv]) <= tol) ++nv;
   hp[g].nvec = nv;
   gp[3 * ng + g].N = nv;

@@ -126,3 +126,19 @@ def test_graph_replay_with_rewritten_angles():
     ref = _run(ops1, n, chi, 1e-8, resident=False)
     assert m.bond_dims == ref.bond_dims
     assert _fid(m, ref) > 1 - 1e-6
+
+
+@pytest.mark.parametrize("resident", [False, True])
+def test_complex64_matches_complex128_before_the_cap_binds(resident):
+    """40-qubit Haar brickwork, first 150 gates (bonds below chi_max = 256, so
+    only the eps = 1e-8 rule truncates): complex64 against complex128 must
+    agree to float32 accuracy in both execution modes.  Guards the eigenvector
+    phase (a too-short inverse iteration once cost 4e-4 here in one mode)."""
+    ops = [op for op in haar_brickwork(40, 20, seed=1234)][:150]
+    a = _run(ops, 40, 256, 1e-8, resident)
+    pol = aq.DTypePolicy(default=torch.complex128)
+    b = aq.AdaptiveMPS(40, bond_dim=1, eps_bond=1e-8, chi_max_per_bond=256, device="cuda",
+                       dtype=torch.complex128, dtype_policy=pol)
+    for _, q, U in ops:
+        b.apply_two_site_gate(q, U)
+    assert _fid(a, b) > 1 - 1e-6
