@@ -136,3 +136,17 @@ def test_circuit_generators_are_deterministic():
     assert count_two_site(h) == 756
     lays = layers_of(a)
     assert len(lays) == 20 and sum(len(x) for x in lays) == 390
+
+
+def test_new_entry_points_validate_arguments_without_a_gpu(lib):
+    """Argument checks run before any CUDA call, so they work on a CPU host."""
+    P = None
+    # batched site mix: bad dtype, null buffers, negative count
+    assert lib.agb_site_mix(7, P, P, P, 1, 4, 4, P) == _lib.AGB_ERR_ARG
+    assert lib.agb_site_mix(_lib.AGB_C64, P, P, P, 1, 4, 4, P) == _lib.AGB_ERR_ARG
+    assert lib.agb_site_mix(_lib.AGB_C64, P, P, P, -1, 4, 4, P) == _lib.AGB_ERR_ARG
+    # asynchronous tensor-core GEMM: the device status word is required
+    assert lib.agb_cgemm_tc_async(b"N", b"N", 1, 8, 8, 8, P, 8, 64, P, 8, 64, P, 8, 64,
+                                  1.0, 0.0, 0.0, 0.0, P, 0, P, P) == _lib.AGB_ERR_ARG
+    # no launch has failed in this process
+    assert lib.agb_last_error() == b""
