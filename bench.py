@@ -547,9 +547,9 @@ def main():
     roof.update({"kernel": dom, "peak_source": src, "stage_ms_per_step": {k: round(v, 3) for k, v in stage_ms.items()},
                  "algorithmic_flops_per_step": wf, "algorithmic_bytes_per_step": wb})
     if dom == "tridiag":
-        # DRAM bytes of one launch from the ncu capture summarised in
-        # profiles/tridiag_cluster_kernel_brickwork40_chi256.md: 20 Gram matrices of
-        # 512 x 512 (one saturated layer), read 14 264 064 B, written 0 B, against
+        # DRAM bytes of one launch from an ncu capture of this kernel on this
+        # workload: 20 Gram matrices of 512 x 512 (one saturated layer), read
+        # 14 264 064 B, written 0 B, against
         # 20 x 2 n^2 x 8 B = 83 886 080 algorithmic bytes (the rest is served from L2,
         # where the Gram GEMM left it)
         roof["traffic"] = 14264064
