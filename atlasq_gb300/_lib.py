@@ -27,9 +27,9 @@ AGB_RUN_REPAIR = 1
 
 # descriptor fields (enum agb_desc_field)
 D_A, D_B, D_U, D_CHIL, D_CHIM, D_CHIR, D_CAP, D_EPS = 0, 1, 2, 3, 4, 5, 6, 7
-D_ANEW, D_BNEW, D_ELL, D_SEED, D_WS = 8, 9, 10, 11, 12
+D_ANEW, D_BNEW, D_ELL, D_SEED, D_WS, D_CTOL = 8, 9, 10, 11, 12, 13
 D_K, D_EPSLOC, D_ENTROPY, D_CONDS, D_STATUS, D_TOTAL, D_NEEDED, D_MODE = 16, 17, 18, 19, 20, 21, 22, 23
-D_DIMS, D_BOND, D_CAPL, D_CAPM, D_CAPR, D_ELLPLAN, D_NVEC = 24, 25, 26, 27, 28, 29, 30
+D_DIMS, D_BOND, D_CAPL, D_CAPM, D_CAPR, D_ELLPLAN, D_NVEC, D_REPAIR = 24, 25, 26, 27, 28, 29, 30, 31
 D_NFIELDS = 32
 
 MLP_NPARAM = 8769
@@ -63,11 +63,13 @@ _SIGS = {
     "agb_two_site_plan": (I, [I, I, P, ctypes.POINTER(SZ)]),
     "agb_two_site_run": (I, [I, I, P, P, I, I, I, I, P, SZ, P, I]),
     "agb_two_site_finalize": (I, [I, I, P, I, I, I, P, P]),
+    "agb_two_site_spectra": (I, [I, I, P, P, I, P, P]),
     "agb_single_qubit_gate": (I, [I, P, P, I, I, P]),
     "agb_single_qubit_batch": (I, [I, I, P, I, P]),
     "agb_tune_tridiag_workspace": (SZ, [I, I, I]),
     "agb_tune_tridiag": (I, [I, I, I, P, SZ, P, P, P]),
     "agb_tuned_tridiag_cluster": (I, [I, I, I]),
+    "agb_set_tridiag_stages": (I, [I]),
     "agb_heevd_workspace": (SZ, [I, I, I]),
     "agb_heevd": (I, [I, I, I, I, P, P, P, P, SZ, U64, P]),
     "agb_qr_workspace": (SZ, [I, I, I]),
@@ -76,13 +78,17 @@ _SIGS = {
     "agb_sample_site": (I, [I, P, I, I, I, U64, U64, P, P, P, P]),
     "agb_mpo_mix": (I, [I, P, P, P, I, I, I, I, P]),
     "agb_trace_prod": (I, [I, P, P, I, P, P]),
+    "agb_mpo_apply_site": (I, [I, P, P, P, I, I, I, I, P]),
+    "agb_tdvp_local_h_workspace": (SZ, [I, I, I, I, I]),
+    "agb_tdvp_local_h": (I, [I, P, P, P, P, P, I, I, I, I, I, I, P, SZ, P]),
     "agb_site_mix": (I, [I, P, P, P, I, I, I, P]),
     "agb_prof_begin": (I, [I]),
     "agb_launch_count": (ctypes.c_longlong, []),
     "agb_last_error": (ctypes.c_char_p, []),
     "agb_prof_end": (I, [P, P, I]),
     "agb_mlp_forward": (I, [P, P, I, P, P]),
-    "agb_mlp_backward": (I, [P, P, P, I, P, P, P]),
+    "agb_mlp_backward_workspace": (SZ, [I]),
+    "agb_mlp_backward": (I, [P, P, P, I, P, P, P, SZ, P]),
     "agb_mlp_adam": (I, [P, P, P, P, I, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                          ctypes.c_float, P]),
     "agb_cgemm_tc_workspace": (SZ, [I, I, I, I]),

@@ -24,7 +24,7 @@ from typing import Dict, List, Optional, Union
 import numpy as np
 import torch
 
-from . import _lib, ops, resident
+from . import _lib, ops, resident, svd_log
 from ._lib import check, dtype_code, ptr, stream_ptr
 from .diagnostics import MPSStatistics
 from .truncation import check_entropy_sanity
@@ -82,6 +82,9 @@ class AdaptiveMPS:
         # optional callable(mps, [(bond, U4x4), ...]) -> list of ell (eigenpairs to compute per gate)
         self.rank_predictor = None
         self.feature_log = None      # list -> (features, k, full) per gate is appended (predictor training data)
+        # SVD-event log (svd_log.py): on when $QIH_SVD_LOG_DIR is set, or assign a logger
+        self.svd_logger = svd_log.get_logger()
+        self.spectrum_log = None     # list -> (step, bond, singular values computed) per gate
         self._last_entropy = {}      # bond -> entanglement entropy at its last update
         self.rank_fallbacks = 0      # gates re-run at full size after a too-small predicted ell
         # device-resident mode (see resident.py): gates run without host synchronisation
@@ -148,7 +151,8 @@ class AdaptiveMPS:
 
     def _maybe_enter_resident(self):
         if (self.device_resident and self._res is None and self.rank_predictor is None
-                and self.budget_global_mb is None and self.feature_log is None):
+                and self.budget_global_mb is None and self.feature_log is None and self.svd_logger is None
+                and self.spectrum_log is None):
             self._drain()
             resident.enter(self)
 
@@ -560,13 +564,14 @@ def apply_gate_entries(entries):
             pe = m.rank_predictor(m, [(entries[g][1], entries[g][2]) for g in idx])
             for g, e in zip(idx, pe):
                 ells[g] = int(e)
-    res = _run_pipeline(entries, dt, ells)
+    spectra = any(m.svd_logger is not None or m.spectrum_log is not None for m, _ in groups.values())
+    res = _run_pipeline(entries, dt, ells, spectra=spectra)
     for m, idx in groups.values():
         m.ell_total += sum(res[g]["ell"] for g in idx)
     # rank fallback: predicted size too small -> rerun those gates at full size
     redo = [g for g, r in enumerate(res) if r["status"] == _lib.AGB_ERR_RANK]
     if redo:
-        full = _run_pipeline([entries[g] for g in redo], dt, None, all_vectors=True)
+        full = _run_pipeline([entries[g] for g in redo], dt, None, all_vectors=True, spectra=spectra)
         for g, r in zip(redo, full):
             r["driver"] = "gb300_gram_heevd_full"
             res[g] = r
@@ -577,7 +582,7 @@ def apply_gate_entries(entries):
                if math.isfinite(r["condS"]) and r["condS"] > entries[g][0].dtype_policy.promote_if_cond_gt
                and dt != _C128]
     if promote:
-        r2 = _run_pipeline([entries[g] for g in promote], _C128, None, all_vectors=True)
+        r2 = _run_pipeline([entries[g] for g in promote], _C128, None, all_vectors=True, spectra=spectra)
         for g, r in zip(promote, r2):
             r["driver"] = "gb300_gram_heevd_c128"
             res[g] = r
@@ -594,6 +599,15 @@ def apply_gate_entries(entries):
             m._last_entropy[i] = r["entropy"]
             if fi is not None:
                 m.feature_log.append((fi[1][0][j], r["k"], int(fi[1][1][j])))
+            if "sigma" in r:
+                if m.spectrum_log is not None:
+                    m.spectrum_log.append((m._operation_counter, i, r["sigma"]))
+                if m.svd_logger is not None:
+                    m.svd_logger.spectrum(bond=i, pre_rank=r["chiM"], chi_max=m.chi_max_per_bond[i], tol=m.eps_bond,
+                                          total_weight=r["total"], sigma=r["sigma"].tolist(), keep=r["k"],
+                                          step=m._operation_counter, chi_left=r["chiL"], chi_right=r["chiR"],
+                                          features=None if fi is None else list(fi[1][0][j]),
+                                          full=None if fi is None else int(fi[1][1][j]))
             if not check_entropy_sanity(r["entropy"], r["chiL"], r["chiR"]):
                 print(f"Warning: Entropy {r['entropy']:.3f} exceeds physical bound at bond {i}")
             m._log_operation(bond=i, k_star=r["k"], chi_before=r["chiM"], chi_after=r["k"],
@@ -601,11 +615,14 @@ def apply_gate_entries(entries):
                              dtype=str(r["dtype"]), ms_elapsed=elapsed, condS=r["condS"])
 
 
-def _run_pipeline(entries, dt, ells, all_vectors=False):
+def _run_pipeline(entries, dt, ells, all_vectors=False, cluster_tol=None, spectra=False):
     """One batched launch sequence: plan -> run -> read ranks -> finalize.
     By default the device computes eigenvectors only for the eigenvalues the
     rank rule can keep (AGB_D_NVEC = 0); ``all_vectors`` computes every one
-    (the re-run of a gate that reported AGB_ERR_RANK).
+    (the re-run of a gate that reported AGB_ERR_RANK).  ``cluster_tol``
+    overrides the eigensolver's relative cluster tolerance (AGB_D_CTOL; the
+    library default is 1e-5).  ``spectra`` also reads back each gate's
+    computed singular values (result key ``sigma``, descending).
     Descriptor rows are built and read with NumPy; the two small copies per
     batch (descriptors up, results down) are the only host synchronisation."""
     lib = _lib.load()
@@ -655,6 +672,8 @@ def _run_pipeline(entries, dt, ells, all_vectors=False):
         desc[:, _lib.D_ELL] = [int(e) for e in ells]
     desc[:, _lib.D_SEED] = cols["seed"]
     desc[:, _lib.D_NVEC] = -1 if all_vectors else 0
+    if cluster_tol is not None:
+        desc[:, _lib.D_CTOL] = _dbits(float(cluster_tol))
     maxL, maxM, maxR = max(cols["L"]), max(cols["M"]), max(cols["R"])
     wsz = _lib.SZ(0)
     check(lib.agb_two_site_plan(code, G, desc.ctypes.data_as(ctypes.c_void_p), ctypes.byref(wsz)),
@@ -668,21 +687,33 @@ def _run_pipeline(entries, dt, ells, all_vectors=False):
     # below the rank, which the caller re-runs at full size
     check(lib.agb_two_site_run(code, G, ptr(desc_dev), ptr(desc_dev), maxL, maxM, maxR, maxell,
                                ptr(ws), wsz.value, stream, _lib.AGB_RUN_REPAIR), "two_site_run")
+    sig = None
+    if spectra:
+        cnt = max(1, maxell)
+        sig_dev = torch.empty(G, cnt, dtype=torch.float64, device=device)
+        check(lib.agb_two_site_spectra(code, G, ptr(desc_dev), ptr(ws), cnt, ptr(sig_dev), stream),
+              "two_site_spectra")
+        sig = sig_dev.cpu().numpy()
     out = desc_dev.cpu().numpy()
     res = []
     maxk = 1
     sts = out[:, _lib.D_STATUS].tolist()
     ks = out[:, _lib.D_K].tolist()
-    reals = np.ascontiguousarray(out[:, [_lib.D_EPSLOC, _lib.D_ENTROPY, _lib.D_CONDS]]).view(np.float64).tolist()
+    reals = np.ascontiguousarray(out[:, [_lib.D_EPSLOC, _lib.D_ENTROPY, _lib.D_CONDS, _lib.D_TOTAL]]
+                                 ).view(np.float64).tolist()
     modes = out[:, _lib.D_MODE].tolist()
     ellv = out[:, _lib.D_ELL].tolist()
+    repv = out[:, _lib.D_REPAIR].tolist()
     for g, (m, i, chiL, chiM, chiR) in enumerate(meta):
         row = out[g]
         st = sts[g]
         k = ks[g]
         r = {"status": st, "k": k, "eps_local": reals[g][0], "entropy": reals[g][1], "condS": reals[g][2],
              "chiL": chiL, "chiM": chiM, "chiR": chiR, "driver": "gb300_gram_heevd", "dtype": dt,
-             "mode": modes[g], "ell": ellv[g]}
+             "mode": modes[g], "ell": ellv[g], "repair": repv[g], "total": reals[g][3]}
+        if sig is not None:
+            row_s = sig[g]
+            r["sigma"] = row_s[:int(np.count_nonzero(row_s))].copy()
         if st not in (_lib.AGB_OK, _lib.AGB_ERR_RANK):
             check(st, f"two-site update on bond {i}")
         ok = m._budget_ok_fn(chiL, chiM, chiR, dt)

@@ -13,6 +13,7 @@ AGB_DEV CX load_op(const CX* P, int64_t ld, int op, int row, int col, int rows, 
   // element (row, col) of op(P), where op(P) is rows x cols
   if (row >= rows || col >= cols) return czero<CX>();
   if (op == 0) return P[(int64_t)row * ld + col];
+  if (op == 3) return cconj(P[(int64_t)row * ld + col]);
   CX v = P[(int64_t)col * ld + row];
   return op == 2 ? cconj(v) : v;
 }
@@ -57,10 +58,10 @@ __global__ void __launch_bounds__(256) gemm_simt_kernel(const GemmProb* __restri
     for (int e = 0; e < 2; ++e) {
       const int idx = tid + e * 256;
       int r, c;
-      if (p.opA == 0) { r = idx / BK; c = idx % BK; } else { r = idx % BM; c = idx / BM; }
+      if (p.opA == 0 || p.opA == 3) { r = idx / BK; c = idx % BK; } else { r = idx % BM; c = idx / BM; }
       As[c][r] = load_op(A, p.lda, p.opA, m0 + r, k0 + c, p.M, p.K);
       int kr, nc;
-      if (p.opB == 0) { kr = idx / BN; nc = idx % BN; } else { kr = idx % BK; nc = idx / BK; }
+      if (p.opB == 0 || p.opB == 3) { kr = idx / BN; nc = idx % BN; } else { kr = idx % BK; nc = idx / BK; }
       Bs[kr][nc] = load_op(B, p.ldb, p.opB, k0 + kr, n0 + nc, p.K, p.N);
     }
     __syncthreads();
@@ -118,7 +119,10 @@ template int launch_gemm_probs<float2>(const GemmProb*, int, int, int, cudaStrea
 template int launch_gemm_probs<double2>(const GemmProb*, int, int, int, cudaStream_t, const GemmCtx*, int);
 
 namespace {
-int op_code(char c) { return (c == 'N' || c == 'n') ? 0 : (c == 'T' || c == 't') ? 1 : (c == 'C' || c == 'c') ? 2 : -1; }
+// 'N' as stored, 'T' transposed, 'C' conjugate-transposed, 'R' conjugated (not transposed)
+int op_code(char c) {
+  return (c == 'N' || c == 'n') ? 0 : (c == 'T' || c == 't') ? 1 : (c == 'C' || c == 'c') ? 2 : (c == 'R' || c == 'r') ? 3 : -1;
+}
 }  // namespace
 
 // Strided-batch host entry (no allocation: the kernel derives each batch

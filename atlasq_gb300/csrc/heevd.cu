@@ -16,6 +16,14 @@ template <> struct rlim<double> {
 
 void heevd_assign_scratch(HeevdProb& p, char* base, int esz) { heevd_assign_scratch_dev(p, base, esz); }
 
+static int g_stages_mode = 1;
+int tridiag_stages_mode() { return g_stages_mode; }
+extern "C" int agb_set_tridiag_stages(int mode) {
+  if (mode != 0 && mode != 1) return AGB_ERR_ARG;
+  g_stages_mode = mode;
+  return AGB_OK;
+}
+
 namespace {
 
 // ------------------------------------------------------------------ stage 1
@@ -192,14 +200,23 @@ __global__ void __launch_bounds__(1024) tridiag_kernel(const HeevdProb* __restri
 }
 
 // ------------------------------------------------------------------ stage 2
+// Number of eigenvalues of T below x (Sturm sequence of the LDL^T pivots).
+// A pivot smaller than pm in magnitude is replaced by -pm BEFORE it is
+// counted, so the count and the recurrence see the same sign (LAPACK dlaebz's
+// order).  Replacing it only at the next step, after counting it as
+// non-negative, loses one eigenvalue whenever a pivot cancels to exactly 0:
+// in float32 that happened at x midway between two leading eigenvalues 1.6e-5
+// apart, bisection then returned a value between them and inverse iteration
+// produced two overlapping eigenvectors.
 template <typename R>
 AGB_DEV int sturm_count(const R* d, const R* e2, int n, R x) {
   const R pm = rlim<R>::pivmin();
   R q = d[0] - x;
+  if (fabs(q) < pm) q = -pm;
   int cnt = q < R(0);
   for (int i = 1; i < n; ++i) {
-    if (fabs(q) < pm) q = -pm;
     q = d[i] - x - e2[i - 1] / q;
+    if (fabs(q) < pm) q = -pm;
     cnt += q < R(0);
   }
   return cnt;
@@ -272,7 +289,7 @@ __global__ void __launch_bounds__(128) invit_kernel(const HeevdProb* __restrict_
   __syncthreads();
   const int t = blockIdx.x * 128 + threadIdx.x;
   if (t >= nv || P.skip_vectors) return;
-  if (in_cluster((const R*)P.lam, nv, t, cluster_tol((const R*)P.lam, ell, cluster_tol_rel(n)))) return;
+  if (in_cluster((const R*)P.lam, nv, t, cluster_tol((const R*)P.lam, ell, P.ctol))) return;
   const R lam = ((const R*)P.lam)[t];
   R tnorm = 0;
   for (int i = 0; i < n; ++i) tnorm = fmax(tnorm, fabs(d[i]) + fabs(e[i]) + (i ? fabs(e[i - 1]) : R(0)));
@@ -654,7 +671,7 @@ __global__ void cluster_list_kernel(const HeevdProb* __restrict__ probs, int cou
     return;
   }
   const R* lam = (const R*)P.lam;
-  const R tol = cluster_tol(lam, ell, cluster_tol_rel(P.n));
+  const R tol = cluster_tol(lam, ell, P.ctol);
   int found = 0, s = 0;
   for (int t = 1; t <= nv; ++t) {
     if (t == nv || (lam[t - 1] - lam[t]) > tol) {
@@ -670,8 +687,7 @@ __global__ void cluster_list_kernel(const HeevdProb* __restrict__ probs, int cou
 }
 
 template <typename R>
-__global__ void __launch_bounds__(256) cluster_invit_kernel(const HeevdProb* __restrict__ probs, double tolrel,
-                                                            int zcap) {
+__global__ void __launch_bounds__(256) cluster_invit_kernel(const HeevdProb* __restrict__ probs, int zcap) {
   const HeevdProb P = probs[blockIdx.y];
   const int n = P.n, ell = P.ell, nv = P.nvec;
   if (nv < 2 || P.skip_vectors) return;
@@ -693,7 +709,6 @@ __global__ void __launch_bounds__(256) cluster_invit_kernel(const HeevdProb* __r
   __shared__ R s_shift, s_nrm;
   const R* lamg = (const R*)P.lam;
   const int tid = threadIdx.x, nt = blockDim.x;
-  (void)tolrel;
   for (int i = tid; i < n; i += nt) {
     d[i] = ((const R*)P.d)[i];
     e[i] = (i < n - 1) ? ((const R*)P.e)[i] : R(0);
@@ -861,12 +876,13 @@ __global__ void __launch_bounds__(256) cluster_invit_kernel(const HeevdProb* __r
 // ------------------------------------------------------------------ stage 5 (backtransform2_kernel below)
 // ------------------------------------------------------------------ stage 6
 // GEMM problems for one Newton-Schulz step: M = Vs^H Vs; Vd = 1.5 Vs - 0.5 Vs M
-__global__ void polish_setup_kernel(const HeevdProb* __restrict__ probs, GemmProb* gp, int count,
+__global__ void polish_setup_kernel(HeevdProb* __restrict__ probs, GemmProb* gp, int count,
                                     int step) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= count) return;
   const HeevdProb P = probs[i];
   const bool fwd = (step == 0);
+  if (fwd && !P.skip_vectors) probs[i].orth_max2 = 0u;
   const void* Vs = fwd ? P.V : P.V2;
   void* Vd = fwd ? P.V2 : P.V;
   const int64_t lds = fwd ? P.ldv : P.ell;
@@ -887,6 +903,42 @@ __global__ void polish_setup_kernel(const HeevdProb* __restrict__ probs, GemmPro
   h.alpha_re = -0.5; h.alpha_im = 0; h.beta_re = 1.5; h.beta_im = 0;
   if (P.skip_vectors) h.M = 0;
   gp[count + i] = h;
+}
+
+// Orthogonality guard on the first polish product M = V^H V (row stride ell).
+// Only eigenvectors whose eigenvalue lies above the float rounding level of
+// the Gram matrix (64 ulp of lambda_0, the level below which the rank rule
+// cannot see a value) are checked: vectors of numerically-zero eigenvalues
+// may mix among themselves and with the others at no cost to X V_k V_k^H,
+// since X maps them to ~0.  The largest |M_ij|^2 over those pairs (i > j)
+// is folded into P.orth_max2 (float bits; atomicMax on non-negative floats
+// orders like the values); a non-finite entry stores +inf.  Two
+// Newton-Schulz steps only reach float32 orthonormality from overlaps below
+// ~1e-2, so a larger value re-runs the problem's vector phase (the two-site
+// repair pass).  Grid: (problems, row groups).
+template <typename CX>
+__global__ void __launch_bounds__(256) orth_guard_kernel(HeevdProb* __restrict__ probs) {
+  typedef typename cx_traits<CX>::R R;
+  HeevdProb& P = probs[blockIdx.x];
+  if (P.skip_vectors) return;
+  const int nv = P.nvec, ell = P.ell;
+  const R* lam = (const R*)P.lam;
+  const R l0 = lam[0];
+  if (!(l0 > R(0))) return;
+  const R floor_ = l0 * R(64) * (sizeof(R) == 4 ? R(5.96e-8) : R(1.11e-16));
+  int kl = 0;
+  while (kl < nv && lam[kl] > floor_) ++kl;  // descending: the checked columns are [0, kl)
+  const CX* M = (const CX*)P.M;
+  float worst = 0.f;
+  for (int i = 1 + blockIdx.y; i < kl; i += gridDim.y)
+    for (int j = threadIdx.x; j < i; j += blockDim.x) {
+      const CX z = M[(int64_t)i * ell + j];
+      const float a2 = (float)cabs2(z);
+      worst = (isfinite(z.x) && isfinite(z.y)) ? fmaxf(worst, a2) : __int_as_float(0x7f800000);
+    }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) worst = fmaxf(worst, __shfl_xor_sync(0xffffffffu, worst, o));
+  if ((threadIdx.x & 31) == 0 && worst > 0.f) atomicMax(&P.orth_max2, __float_as_uint(worst));
 }
 
 // V = Q Y, reflectors applied in pairs (j, j-1), each pair staged once per CTA
@@ -1026,14 +1078,21 @@ int launch_heevd_values(HeevdProb* probs, int count, int maxn, int maxell, cudaS
     attr_set[esz == 16] = true;
   }
   prof_mark(AGB_ST_TRIDIAG, s);
-  // cluster kernel (rows in distributed shared memory, overflow rows in L2);
-  // the single-CTA kernel only if the device refuses the cluster launch
+  // two-stage reduction (band on a cluster, then bulge chasing) where the band
+  // fits; else the one-stage cluster kernel (rows in distributed shared memory,
+  // overflow rows in L2); the single-CTA kernel only if the device refuses the
+  // cluster launch
+  if (tridiag_stages_mode() == 0 && two_stage_bw(esz, maxn) > 0) {
+    const int rc2 = launch_two_stage<CX>(probs, count, maxn, s);
+    if (rc2 != AGB_OK) return rc2;
+  } else {
   const int rc0 = tridiag_cluster_size(esz, maxn) > 0 ? launch_tridiag_cluster<CX>(probs, count, maxn, s)
                                                       : AGB_ERR_UNSUPPORTED;
   if (rc0 != AGB_OK) {
     cudaGetLastError();
     tridiag_kernel<CX><<<count, 1024, sm_tri, s>>>(probs);
     AGB_CHECK_LAUNCH();
+  }
   }
   if (maxell <= 0) return AGB_OK;
   const size_t sm_r = 2 * (size_t)maxn * sizeof(R);
@@ -1069,12 +1128,14 @@ int launch_heevd_vectors(HeevdProb* probs, GemmProb* gp, int count, int maxn, in
     const int maxcl = maxell / 2 > 0 ? maxell / 2 : 1;
     cluster_list_kernel<R><<<(count + 127) / 128, 128, 0, s>>>(probs, count);
     AGB_CHECK_LAUNCH();
-    cluster_invit_kernel<R><<<dim3(maxcl, count), 256, sm, s>>>(probs, cluster_tol_rel(maxn), zcap);
+    cluster_invit_kernel<R><<<dim3(maxcl, count), 256, sm, s>>>(probs, zcap);
     AGB_CHECK_LAUNCH();
   }
   int rc;
   prof_mark(AGB_ST_BACKTRANS, s);
-  if (maxn <= 128) rc = launch_bt<CX, 4>(probs, count, maxell, s);
+  if (tridiag_stages_mode() == 0 && two_stage_bw(sizeof(CX), maxn) > 0)
+    rc = launch_bt_two_stage<CX>(probs, count, maxn, maxell, s);
+  else if (maxn <= 128) rc = launch_bt<CX, 4>(probs, count, maxell, s);
   else if (maxn <= 256) rc = launch_bt<CX, 8>(probs, count, maxell, s);
   else if (maxn <= 512) rc = launch_bt<CX, 16>(probs, count, maxell, s);
   else rc = launch_bt<CX, 32>(probs, count, maxell, s);
@@ -1088,6 +1149,10 @@ int launch_heevd_vectors(HeevdProb* probs, GemmProb* gp, int count, int maxn, in
     polish_setup_kernel<<<(count + 127) / 128, 128, 0, s>>>(probs, gp, count, step & 1);
     AGB_CHECK_LAUNCH();
     if ((rc = launch_gemm_probs<CX>(gp, count, maxell, maxell, s, ctx, maxn))) return rc;
+    if (step == 0) {
+      orth_guard_kernel<CX><<<dim3(count, 8), 256, 0, s>>>(probs);
+      AGB_CHECK_LAUNCH();
+    }
     if ((rc = launch_gemm_probs<CX>(gp + count, count, maxn, maxell, s, ctx, maxell))) return rc;
   }
   return AGB_OK;
@@ -1125,6 +1190,9 @@ __global__ void heevd_setup_kernel(HeevdProb* probs, void* H, void* evecs, char*
   p.skip_vectors = 0;
   p.nvec = ell;
   p.redo = 0;
+  p.orth_max2 = 0u;
+  p.ctol = kClusterTol;
+  p.fail = 0;
   heevd_assign_scratch_dev(p, scratch + (size_t)b * scratch_stride, esz);
   probs[b] = p;
 }

@@ -16,18 +16,27 @@
 #pragma once
 #include "gemm.cuh"
 
-// Eigenvalues closer than cluster_tol_rel(n) * max|lambda| are solved as a
-// cluster (re-orthogonalised inverse iteration); wider gaps leave
-// inverse-iteration vectors close enough to orthogonal for the Newton-Schulz
-// polish.  Measured on a Trotter-Ising two-site update (58 x 56, ten leading
-// eigenvalues 1e-5..4e-5 apart): at 1e-5, two vectors collapsed onto one
-// direction for 78% of random starts, dropping a leading singular vector
-// (relative error 0.26); at 1e-4, 3 of 400 starts; at 1e-3 (LAPACK stein's
-// ortol) none.  On the dense spectra of large Gram matrices (n >= 512) gaps
-// below 1e-4 chain into clusters of hundreds of members, which makes the
-// cluster stage several times slower, so those keep 1e-5 (with the remaining
-// risk described in the design notes).
-AGB_HD double cluster_tol_rel(int n) { return n <= 256 ? 1e-3 : 1e-5; }
+// Eigenvalues closer than kClusterTol * max|lambda| are solved as a cluster
+// (re-orthogonalised inverse iteration, LAPACK stein's scheme); wider gaps
+// leave inverse-iteration vectors within ~(bisection error / gap)^3 of
+// orthogonal, far below what the Newton-Schulz polish removes.  A problem whose
+// first polish product V^H V still shows an overlap above kOrthGuard (two
+// polish steps reach float32 orthonormality only from overlaps below ~1e-2)
+// has its vector phase re-run with the wider kClusterTolWide (the repair pass
+// of the two-site pipeline).  On dense spectra of large Gram matrices
+// (n >= 512) the wide tolerance chains hundreds of eigenvalues into one
+// cluster, so it is only a repair setting.
+constexpr double kClusterTol = 1e-5;
+constexpr double kClusterTolWide = 1e-3;
+constexpr float kOrthGuard = 1e-2f;
+AGB_HD bool orth_exceeds(unsigned max2_bits) {
+  union {
+    unsigned u;
+    float f;
+  } c;
+  c.u = max2_bits;
+  return !(c.f <= kOrthGuard * kOrthGuard);  // NaN / inf included
+}
 
 struct HeevdProb {
   void* H;       // CX[n x ldh], Hermitian input, overwritten by the reduction
@@ -49,7 +58,26 @@ struct HeevdProb {
   int nvec;          // eigenvectors to compute (the leading nvec of the ell eigenvalues), <= ell;
                      // may be lowered between the two phases; strides stay ell
   int redo;          // set by the two-site repair pass: this problem's vector phase runs again
+  unsigned orth_max2;  // orthogonality guard: largest |(V^H V)_ij|^2 over the checked pairs (float bits)
+  double ctol;       // cluster tolerance relative to max|lambda| (kClusterTol unless repaired)
+  void* band;        // scratch of the two-stage tridiagonalisation (block-reflector factors,
+                     // exchange rows, band-stage reflectors), tridiag_2stage.cu
+  int fail;          // set when a bounded wait of the band stage expired
 };
+
+// Bytes of the two-stage scratch for an n x n problem (the larger of the band
+// widths the launcher may choose).
+AGB_HD size_t two_stage_scratch_bytes(int esz, int n) {
+  size_t best = 0;
+  for (int bw = 8; bw <= 16; bw *= 2) {
+    const size_t np = (size_t)(n + bw - 1) / bw;
+    const size_t km = (size_t)((n - 1 + bw - 1) / bw > 0 ? (n - 1 + bw - 1) / bw : 1);
+    const size_t b = agb_align(np * bw * bw * esz) + agb_align((size_t)n * bw * esz) +
+                     agb_align((size_t)n * km * bw * esz) + agb_align((size_t)n * km * esz);
+    if (b > best) best = b;
+  }
+  return best;
+}
 
 // Bytes of per-problem scratch (d, e, tau, lam, Y, lu, V2, M, scale) for one
 // problem of size n with ell eigenpairs; V and H are not included.
@@ -68,16 +96,28 @@ AGB_HD void heevd_assign_scratch_dev(HeevdProb& p, char* base, int esz) {
   p.V2 = base + o;    o += agb_align(n * ell * esz);
   p.M = base + o;     o += agb_align(ell * ell * esz);
   p.scale = base + o; o += agb_align(rsz);
+  p.band = base + o;  o += agb_align(two_stage_scratch_bytes(esz, p.n));
 }
 
 AGB_HD size_t heevd_scratch_bytes(int esz, int n, int ell) {
   const int rsz = esz / 2;
   const size_t N = n, L = ell;
   return agb_align(N * rsz) * 2 + agb_align(N * esz) + agb_align(L * rsz) + agb_align(N * L * rsz) +
-         agb_align(5 * N * L * rsz) + agb_align(N * L * esz) + agb_align(L * L * esz) + agb_align(rsz);
+         agb_align(5 * N * L * rsz) + agb_align(N * L * esz) + agb_align(L * L * esz) + agb_align(rsz) +
+         agb_align(two_stage_scratch_bytes(esz, n));
 }
 
 
+
+// Two-stage tridiagonalisation (tridiag_2stage.cu): band width for a batch
+// (0 = not applicable), stage 1 + 2, and the matching back-transformation.
+int two_stage_bw(int esz, int maxn);
+template <typename CX>
+int launch_two_stage(HeevdProb* probs, int count, int maxn, cudaStream_t s);
+template <typename CX>
+int launch_bt_two_stage(const HeevdProb* probs, int count, int maxn, int maxell, cudaStream_t s);
+// 0: two-stage where it applies, 1 (default): always the one-stage kernels.
+int tridiag_stages_mode();
 
 // Cluster (distributed shared memory) tridiagonalisation, tridiag_cluster.cu.
 size_t tridiag_cluster_smem(int esz, int n, int C);

@@ -64,18 +64,21 @@ __global__ void __launch_bounds__(128) mlp_forward_kernel(const float* __restric
   Y[b] = sigmoid(forward_one(sp, x, h1, h2, h3));
 }
 
-// Forward + backward of the MSE loss for a batch; grads (NPARAM floats) are
-// accumulated (the caller zeroes them); loss_sum (one float) gets sum_b (y-t)^2.
-// Every lane of a warp walks the same weights in the same order (threads past
-// the batch carry zero error), so each per-weight contribution is reduced
-// across the warp with shuffles and added to the block gradient by lane 0.
-__global__ void __launch_bounds__(128) mlp_backward_kernel(const float* __restrict__ params, const float* __restrict__ X,
-                                                           const float* __restrict__ T, int B, float inv_batch,
-                                                           float* __restrict__ grads, float* __restrict__ loss_sum) {
+// Forward + backward of the MSE loss for a batch, deterministic: every warp
+// accumulates its lanes' contributions (warp shuffles, a fixed tree) into its
+// own slice of shared memory, the block adds its four slices in warp order and
+// writes one partial gradient row (and partial loss) per block to `part`;
+// mlp_reduce_kernel then adds the rows in block order.  No float atomics, so a
+// training run is reproducible bit for bit.
+constexpr int BW = 128, NWARP = BW / 32;
+__global__ void __launch_bounds__(BW) mlp_backward_kernel(const float* __restrict__ params, const float* __restrict__ X,
+                                                          const float* __restrict__ T, int B, float inv_batch,
+                                                          float* __restrict__ part, float* __restrict__ part_loss) {
   extern __shared__ float smem_f[];
-  float* sp = smem_f;          // [NPARAM]
-  float* sg = smem_f + NPARAM;  // [NPARAM] block gradient
-  for (int i = threadIdx.x; i < NPARAM; i += blockDim.x) sg[i] = 0.f;
+  float* sp = smem_f;                              // [NPARAM]
+  const int wid = threadIdx.x >> 5;
+  float* sgw = smem_f + NPARAM * (1 + wid);       // this warp's gradient slice [NPARAM]
+  for (int i = threadIdx.x; i < NWARP * NPARAM; i += blockDim.x) smem_f[NPARAM + i] = 0.f;
   load_params(params, sp);
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   const bool lane0 = (threadIdx.x & 31) == 0;
@@ -90,12 +93,12 @@ __global__ void __launch_bounds__(128) mlp_backward_kernel(const float* __restri
   // layer 4: z = W4 h3 + b4
   {
     const float r = warp_sum(dz);
-    if (lane0) atomicAdd(&sg[OFF_B4], r);
+    if (lane0) sgw[OFF_B4] += r;
   }
   float d3[H];
   for (int i = 0; i < H; ++i) {
     const float r = warp_sum(dz * h3[i]);
-    if (lane0) atomicAdd(&sg[OFF_W4 + i], r);
+    if (lane0) sgw[OFF_W4 + i] += r;
     d3[i] = (h3[i] > 0.f) ? dz * sp[OFF_W4 + i] : 0.f;
   }
   // layer 3: h3 = relu(W3 h2 + b3)
@@ -104,10 +107,10 @@ __global__ void __launch_bounds__(128) mlp_backward_kernel(const float* __restri
   for (int o = 0; o < H; ++o) {
     const float g = d3[o];
     const float rb = warp_sum(g);
-    if (lane0) atomicAdd(&sg[OFF_B3 + o], rb);
+    if (lane0) sgw[OFF_B3 + o] += rb;
     for (int i = 0; i < H; ++i) {
       const float r = warp_sum(g * h2[i]);
-      if (lane0) atomicAdd(&sg[OFF_W3 + o * H + i], r);
+      if (lane0) sgw[OFF_W3 + o * H + i] += r;
       d2[i] = fmaf(g, sp[OFF_W3 + o * H + i], d2[i]);
     }
   }
@@ -119,10 +122,10 @@ __global__ void __launch_bounds__(128) mlp_backward_kernel(const float* __restri
   for (int o = 0; o < H; ++o) {
     const float g = d2[o];
     const float rb = warp_sum(g);
-    if (lane0) atomicAdd(&sg[OFF_B2 + o], rb);
+    if (lane0) sgw[OFF_B2 + o] += rb;
     for (int i = 0; i < H; ++i) {
       const float r = warp_sum(g * h1[i]);
-      if (lane0) atomicAdd(&sg[OFF_W2 + o * H + i], r);
+      if (lane0) sgw[OFF_W2 + o * H + i] += r;
       d1[i] = fmaf(g, sp[OFF_W2 + o * H + i], d1[i]);
     }
   }
@@ -130,19 +133,39 @@ __global__ void __launch_bounds__(128) mlp_backward_kernel(const float* __restri
   for (int o = 0; o < H; ++o) {
     const float g = (h1[o] > 0.f) ? d1[o] : 0.f;
     const float rb = warp_sum(g);
-    if (lane0) atomicAdd(&sg[OFF_B1 + o], rb);
+    if (lane0) sgw[OFF_B1 + o] += rb;
 #pragma unroll
     for (int i = 0; i < IN; ++i) {
       const float r = warp_sum(g * x[i]);
-      if (lane0) atomicAdd(&sg[OFF_W1 + o * IN + i], r);
+      if (lane0) sgw[OFF_W1 + o * IN + i] += r;
     }
   }
   __shared__ float red[32];
-  const float tot = block_sum(live ? err2 : 0.f, red);
-  __syncthreads();
-  for (int i = threadIdx.x; i < NPARAM; i += blockDim.x)
-    if (sg[i] != 0.f) atomicAdd(&grads[i], sg[i]);
-  if (threadIdx.x == 0 && loss_sum) atomicAdd(loss_sum, tot);
+  const float tot = block_sum(live ? err2 : 0.f, red);  // fixed tree (ends with a barrier)
+  float* row = part + (int64_t)blockIdx.x * NPARAM;
+  for (int i = threadIdx.x; i < NPARAM; i += blockDim.x) {
+    float acc = 0.f;
+#pragma unroll
+    for (int w = 0; w < NWARP; ++w) acc += smem_f[NPARAM * (1 + w) + i];
+    row[i] = acc;
+  }
+  if (threadIdx.x == 0) part_loss[blockIdx.x] = tot;
+}
+
+// grads[i] = sum over blocks (in block order) of part[block][i]; loss likewise.
+__global__ void mlp_reduce_kernel(const float* __restrict__ part, const float* __restrict__ part_loss, int nblocks,
+                                  float* __restrict__ grads, float* __restrict__ loss_sum) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < NPARAM) {
+    float acc = 0.f;
+    for (int b = 0; b < nblocks; ++b) acc += part[(int64_t)b * NPARAM + i];
+    grads[i] = acc;
+  }
+  if (i == 0 && loss_sum) {
+    float l = 0.f;
+    for (int b = 0; b < nblocks; ++b) l += part_loss[b];
+    *loss_sum = l;
+  }
 }
 
 // Adam with decoupled weight decay (AdamW): m = b1 m + (1-b1) g; v = b2 v + (1-b2) g^2;
@@ -171,20 +194,28 @@ extern "C" int agb_mlp_forward(const float* params, const float* X, int B, float
   return AGB_OK;
 }
 
+extern "C" size_t agb_mlp_backward_workspace(int B) {
+  const size_t nb = B > 0 ? (size_t)(B + BW - 1) / BW : 0;
+  return agb_align(nb * NPARAM * sizeof(float)) + agb_align(nb * sizeof(float));
+}
+
 extern "C" int agb_mlp_backward(const float* params, const float* X, const float* T, int B, float* grads,
-                                float* loss_sum, void* stream) {
-  if (!params || !X || !T || !grads || B <= 0) return AGB_ERR_ARG;
+                                float* loss_sum, void* ws, size_t ws_bytes, void* stream) {
+  if (!params || !X || !T || !grads || B <= 0 || !ws) return AGB_ERR_ARG;
+  if (ws_bytes < agb_mlp_backward_workspace(B)) return AGB_ERR_WORKSPACE;
   cudaStream_t s = (cudaStream_t)stream;
-  if (cudaMemsetAsync(grads, 0, NPARAM * sizeof(float), s) != cudaSuccess) return AGB_ERR_CUDA;
-  if (loss_sum && cudaMemsetAsync(loss_sum, 0, sizeof(float), s) != cudaSuccess) return AGB_ERR_CUDA;
-  const size_t smem = 2 * NPARAM * sizeof(float);
-  static bool attr = false;
-  if (!attr) {
-    if (cudaFuncSetAttribute(mlp_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-      return AGB_ERR_CUDA;
-    attr = true;
+  const int nb = (B + BW - 1) / BW;
+  float* part = (float*)ws;
+  float* part_loss = (float*)((char*)ws + agb_align((size_t)nb * NPARAM * sizeof(float)));
+  const size_t smem = (size_t)(1 + NWARP) * NPARAM * sizeof(float);
+  const cudaError_t oe = agb_smem_optin(mlp_backward_kernel, smem);
+  if (oe != cudaSuccess) {
+    agb_note_error(__FILE__, __LINE__, oe);
+    return AGB_ERR_CUDA;
   }
-  mlp_backward_kernel<<<(B + 127) / 128, 128, smem, s>>>(params, X, T, B, 1.f / (float)B, grads, loss_sum);
+  mlp_backward_kernel<<<nb, BW, smem, s>>>(params, X, T, B, 1.f / (float)B, part, part_loss);
+  AGB_CHECK_LAUNCH();
+  mlp_reduce_kernel<<<(NPARAM + 255) / 256, 256, 0, s>>>(part, part_loss, nb, grads, loss_sum);
   AGB_CHECK_LAUNCH();
   return AGB_OK;
 }

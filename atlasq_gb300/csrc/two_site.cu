@@ -91,6 +91,7 @@ __global__ void setup_kernel(int64_t* __restrict__ desc, int ng, char* ws, int e
   if (g >= ng) return;
   int64_t* D = desc + (int64_t)g * AGB_D_NFIELDS;
   D[AGB_D_STATUS] = AGB_OK;
+  D[AGB_D_REPAIR] = 0;
   if (D[AGB_D_DIMS]) {
     // device-resident MPS: the shapes are whatever earlier launches left in the
     // bond-dimension array, bounded by the capacities the batch was planned
@@ -130,6 +131,9 @@ __global__ void setup_kernel(int64_t* __restrict__ desc, int ng, char* ws, int e
   p.skip_vectors = 0;
   p.nvec = ell;
   p.redo = 0;
+  p.orth_max2 = 0u;
+  p.fail = 0;
+  p.ctol = D[AGB_D_CTOL] ? dbits(D[AGB_D_CTOL]) : kClusterTol;
   heevd_assign_scratch_dev(p, slab + L.heevd, esz);
   hp[g] = p;
   // gp[0..2ng) reserved for the eigensolver polish; [2ng, 3ng) Gram; [3ng, 4ng) AV
@@ -413,7 +417,7 @@ __global__ void __launch_bounds__(512) prerank_kernel(int64_t* __restrict__ desc
   if (nv >= ell) return;
   // do not split a cluster (the tolerance of the cluster kernel)
   const R scl = fmax(fabs(lam[0]), fabs(lam[ell - 1]));
-  const R tol = (R)cluster_tol_rel(n) * fmax(scl, (R)(sizeof(R) == 4 ? 1e-30 : 1e-290));
+  const R tol = (R)P.ctol * fmax(scl, (R)(sizeof(R) == 4 ? 1e-30 : 1e-290));
   while (nv < ell && (lam[nv - 1] - lam[nv]) <= tol) ++nv;
   hp[g].nvec = nv;
   gp[3 * ng + g].N = nv;
@@ -425,11 +429,14 @@ __global__ void __launch_bounds__(512) prerank_kernel(int64_t* __restrict__ desc
 //   E = cumsum(S*S) accumulated in double, each partial rounded to float32;
 //   thresh = f32(f32(1 - eps^2) * total); k_tol = searchsorted_left(E, thresh) + 1.
 template <typename CX>
-__global__ void __launch_bounds__(1024) rank_kernel(int64_t* __restrict__ desc, int ng, char* ws, int only_redo) {
+// pass: 0 first pass (a repair pass follows), 1 repair pass (only repaired
+// gates), 2 first pass with no repair pass.  In passes 1 and 2 a gate whose
+// eigenvectors failed the orthogonality guard reports AGB_ERR_NOCONV.
+__global__ void __launch_bounds__(1024) rank_kernel(int64_t* __restrict__ desc, int ng, char* ws, int pass) {
   typedef typename cx_traits<CX>::R R;
   const bool f32 = sizeof(R) == 4;
   const int g = blockIdx.x;
-  if (only_redo && !((const HeevdProb*)ws)[g].redo) return;
+  if (pass == 1 && !((const HeevdProb*)ws)[g].redo) return;
   int64_t* D = desc + (int64_t)g * AGB_D_NFIELDS;
   const int chiL = (int)D[AGB_D_CHIL], chiR = (int)D[AGB_D_CHIR];
   const int m = 2 * chiL, n = 2 * chiR, ell = (int)D[AGB_D_ELL], cap = (int)D[AGB_D_CAP];
@@ -526,6 +533,14 @@ __global__ void __launch_bounds__(1024) rank_kernel(int64_t* __restrict__ desc, 
     status = AGB_ERR_NOCONV;
     k = 0;
   }
+  if (pass != 0 && orth_exceeds(hp[g].orth_max2) && mode0 != 1) {  // eigenvectors not orthonormal, no repair left
+    status = AGB_ERR_NOCONV;
+    k = 0;
+  }
+  if (hp[g].fail) {  // a bounded wait of the band stage expired
+    status = AGB_ERR_TIMEOUT;
+    k = 0;
+  }
   if (*status_word(ws, ng) != 0) {  // a bounded wait in a tensor-core GEMM expired
     status = *status_word(ws, ng);
     k = 0;
@@ -590,10 +605,34 @@ __global__ void scatter_kernel(const int64_t* __restrict__ desc, char* ws) {
   }
 }
 
+// Singular values of each gate of the last run, descending: out[g][t] =
+// sqrt(sigma^2_t) for the values the run computed (t < nvec, every ell in the
+// identity mode), zero beyond them, `count` entries per gate.  A gate that
+// failed (status other than OK / RANK) reports zeros.
+__global__ void spectra_kernel(const int64_t* __restrict__ desc, const char* ws, int esz, int count,
+                               double* __restrict__ out) {
+  const int g = blockIdx.y;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  const int64_t* D = desc + (int64_t)g * AGB_D_NFIELDS;
+  const int chiL = (int)D[AGB_D_CHIL], chiR = (int)D[AGB_D_CHIR], ell = (int)D[AGB_D_ELL];
+  const int st = (int)D[AGB_D_STATUS];
+  const HeevdProb* hp = (const HeevdProb*)ws;
+  const int nv = (D[AGB_D_MODE] == 1) ? ell : min(hp[g].nvec, ell);
+  double v = 0.0;
+  if ((st == AGB_OK || st == AGB_ERR_RANK) && t < nv) {
+    const Slab Ls = slab_layout(2 * chiL, 2 * chiR, ell, esz);
+    const double s2 = ((const double*)(ws + D[AGB_D_WS] + Ls.sig2))[t];
+    v = s2 > 0.0 ? sqrt(s2) : 0.0;
+  }
+  out[(int64_t)g * count + t] = v;
+}
+
 // Repair pass (on the device, no host round trip): a gate whose eigenvector
 // phase was cut short by the eigenvalue-guided count (AGB_ERR_RANK with
-// nvec < ell) runs its vector phase, X*V and rank selection again with every
-// vector; every other gate is skipped by those launches.
+// nvec < ell), or whose eigenvectors failed the orthogonality guard (then with
+// the wide cluster tolerance), runs its vector phase, X*V and rank selection
+// again with every vector; every other gate is skipped by those launches.
 __global__ void repair_setup_kernel(int64_t* __restrict__ desc, int ng, char* ws) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= ng) return;
@@ -601,13 +640,18 @@ __global__ void repair_setup_kernel(int64_t* __restrict__ desc, int ng, char* ws
   HeevdProb* hp = (HeevdProb*)ws;
   GemmProb* gp = (GemmProb*)(ws + agb_align((size_t)ng * sizeof(HeevdProb)));
   const int ell = (int)D[AGB_D_ELL];
-  if (D[AGB_D_STATUS] == AGB_ERR_RANK && hp[g].nvec < ell && D[AGB_D_MODE] == 0) {
+  const int st = (int)D[AGB_D_STATUS];
+  const bool short_count = st == AGB_ERR_RANK && hp[g].nvec < ell && D[AGB_D_MODE] == 0;
+  const bool overlap = orth_exceeds(hp[g].orth_max2) && D[AGB_D_MODE] == 0 && (st == AGB_OK || st == AGB_ERR_RANK);
+  if (short_count || overlap) {
     hp[g].redo = 1;
     hp[g].nvec = ell;
     hp[g].skip_vectors = 0;
+    if (overlap) hp[g].ctol = kClusterTolWide;
     gp[3 * ng + g].N = ell;
     gp[3 * ng + g].M = 2 * (int)D[AGB_D_CHIL];
     D[AGB_D_STATUS] = AGB_OK;
+    D[AGB_D_REPAIR] = (short_count ? 1 : 0) | (overlap ? 2 : 0);
   } else {
     hp[g].redo = 0;
     hp[g].skip_vectors = 1;
@@ -649,7 +693,8 @@ int run_impl(int ng, int64_t* desc, int maxL, int maxM, int maxR, int maxell, ch
   rc = launch_gemm_probs<CX>(gp + 3 * ng, ng, maxm, maxell, s, &ctx, maxn);
   if (rc) return rc;
   prof_mark(AGB_ST_RANK, s);
-  rank_kernel<CX><<<ng, 1024, 4 * (size_t)maxell * sizeof(double), s>>>(desc, ng, ws, 0);
+  rank_kernel<CX><<<ng, 1024, 4 * (size_t)maxell * sizeof(double), s>>>(desc, ng, ws,
+                                                                          (flags & AGB_RUN_REPAIR) ? 0 : 2);
   AGB_CHECK_LAUNCH();
   if (!(flags & AGB_RUN_REPAIR)) {
     prof_mark(AGB_ST_GAP, s);
@@ -764,5 +809,18 @@ extern "C" int agb_two_site_finalize(int dtype, int ng, const int64_t* desc_dev,
   else scatter_kernel<double2><<<dim3(blocks, ng), 256, 0, s>>>(desc_dev, (char*)ws);
   AGB_CHECK_LAUNCH();
   prof_mark(AGB_ST_GAP, s);
+  return AGB_OK;
+}
+
+extern "C" int agb_two_site_spectra(int dtype, int ng, const int64_t* desc_dev, const void* ws, int count,
+                                    double* out, void* stream) {
+  if (dtype != AGB_C64 && dtype != AGB_C128) return AGB_ERR_ARG;
+  if (ng < 0 || count < 0) return AGB_ERR_ARG;
+  if (ng == 0 || count == 0) return AGB_OK;
+  if (!desc_dev || !ws || !out || ng > 65535) return AGB_ERR_ARG;
+  const int esz = dtype == AGB_C64 ? 8 : 16;
+  spectra_kernel<<<dim3((count + 127) / 128, ng), 128, 0, (cudaStream_t)stream>>>(desc_dev, (const char*)ws, esz,
+                                                                                 count, out);
+  AGB_CHECK_LAUNCH();
   return AGB_OK;
 }

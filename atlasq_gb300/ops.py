@@ -53,8 +53,8 @@ def cgemm(A, B, opA="N", opB="N", alpha=1.0, beta=0.0, C=None):
     bat = A2.shape[0]
     ra, ca = A2.shape[1], A2.shape[2]
     rb, cb = B2.shape[1], B2.shape[2]
-    M, K = (ra, ca) if opA == "N" else (ca, ra)
-    K2, N = (rb, cb) if opB == "N" else (cb, rb)
+    M, K = (ra, ca) if opA in ("N", "R") else (ca, ra)
+    K2, N = (rb, cb) if opB in ("N", "R") else (cb, rb)
     if K != K2:
         raise ValueError(f"inner dimension mismatch {K} vs {K2}")
     if C is None:
@@ -68,6 +68,24 @@ def cgemm(A, B, opA="N", opB="N", alpha=1.0, beta=0.0, C=None):
                                 ptr(A2), ca, ra * ca, ptr(B2), cb, rb * cb, ptr(C), N, M * N,
                                 al.real, al.imag, be.real, be.imag, stream_ptr(A.device)), "cgemm")
     return C if batched else C[0]
+
+
+def cgemm_strided(batch, M, N, K, A, a_off, lda, sA, B, b_off, ldb, sB, C, c_off, ldc, sC, opA="N", opB="N",
+                  alpha=1.0, beta=0.0):
+    """Strided-batch GEMM on raw layouts: batch entry z uses A from element
+    a_off + z * sA with row stride lda (likewise B, C); op(A) is M x K, op(B)
+    K x N.  Lets a contraction read and write a permuted index order in place."""
+    lib = _lib.load()
+    for t in (A, B, C):
+        _c(t)
+    es = A.element_size()
+    al, be = complex(alpha), complex(beta)
+    check(lib.agb_cgemm_batched(dtype_code(A.dtype), opA.encode(), opB.encode(), batch, M, N, K,
+                                ctypes.c_void_p(A.data_ptr() + a_off * es), lda, sA,
+                                ctypes.c_void_p(B.data_ptr() + b_off * es), ldb, sB,
+                                ctypes.c_void_p(C.data_ptr() + c_off * es), ldc, sC,
+                                al.real, al.imag, be.real, be.imag, stream_ptr(A.device)), "cgemm_strided")
+    return C
 
 
 def heevd(H, ell=None, seed=0):
@@ -153,8 +171,8 @@ def cgemm_tc(A, B, opA="N", opB="N", alpha=1.0, beta=0.0, C=None, sync=True):
     bat = A2.shape[0]
     ra, ca = A2.shape[1], A2.shape[2]
     rb, cb = B2.shape[1], B2.shape[2]
-    M, K = (ra, ca) if opA == "N" else (ca, ra)
-    K2, N = (rb, cb) if opB == "N" else (cb, rb)
+    M, K = (ra, ca) if opA in ("N", "R") else (ca, ra)
+    K2, N = (rb, cb) if opB in ("N", "R") else (cb, rb)
     if K != K2:
         raise ValueError(f"inner dimension mismatch {K} vs {K2}")
     if C is None:

@@ -27,7 +27,7 @@ import math
 import numpy as np
 import torch
 
-from . import _lib
+from . import _lib, ops
 from ._lib import check, ptr, stream_ptr
 
 NPARAM = _lib.MLP_NPARAM
@@ -114,8 +114,10 @@ class RankPredictor:
         Td = torch.as_tensor(np.ascontiguousarray(T, dtype=np.float32)).to(self.device)
         grads = torch.empty(NPARAM, dtype=torch.float32, device=self.device)
         loss = torch.empty(1, dtype=torch.float32, device=self.device)
+        need = lib.agb_mlp_backward_workspace(Xd.shape[0])
+        ws = ops.workspace(need, self.device, "mlp")
         check(lib.agb_mlp_backward(ptr(self.params), ptr(Xd), ptr(Td), Xd.shape[0], ptr(grads), ptr(loss),
-                                   stream_ptr(self.device)), "mlp_backward")
+                                   ptr(ws), ws.numel(), stream_ptr(self.device)), "mlp_backward")
         return loss / Xd.shape[0], grads
 
     def train(self, X, T, steps=400, batch=512, lr=3e-3, weight_decay=1e-5, seed=0):

@@ -57,6 +57,8 @@ enum agb_desc_field {
   AGB_D_ELL = 10,     /* (in)  eigenpairs to compute; 0 = min(2chiR, cap)      */
   AGB_D_SEED = 11,    /* (in)  Philox seed for start vectors                   */
   AGB_D_WS = 12,      /* (plan) byte offset of this gate's workspace slab      */
+  AGB_D_CTOL = 13,    /* (in)  eigenvalue cluster tolerance relative to the largest
+                       *       eigenvalue (double bits); 0 = the default 1e-5     */
   AGB_D_K = 16,       /* (out) kept rank                                       */
   AGB_D_EPSLOC = 17,  /* (out) eps_local (double bits)                         */
   AGB_D_ENTROPY = 18, /* (out) entropy in nats (double bits)                   */
@@ -80,6 +82,9 @@ enum agb_desc_field {
   AGB_D_ELLPLAN = 29, /* (plan) planned eigenpair count (with DIMS)            */
   AGB_D_NVEC = 30,    /* (in)  0: eigenvectors only for the values the rank rule can
                        *       keep (from the eigenvalues, plus a pad); -1: all ell */
+  AGB_D_REPAIR = 31,  /* (out) vector phase re-run on the device: bit 0 the guided
+                       *       count fell short, bit 1 the eigenvectors failed the
+                       *       orthogonality guard (re-run with tolerance 1e-3)   */
   AGB_D_NFIELDS = 32
 };
 
@@ -109,13 +114,23 @@ int agb_contract_gate(int dtype, const void* A, const void* B, const void* U, vo
  *                     AGB_D_ANEW / AGB_D_BNEW buffers sized from AGB_D_K. */
 int agb_two_site_plan(int dtype, int ngates, int64_t* desc_host, size_t* ws_bytes);
 #define AGB_RUN_REPAIR 1 /* flags: re-run, on the device, the vector phase of gates whose
-                          * eigenvalue-guided eigenvector count fell short (AGB_D_NVEC = 0);
-                          * without it such gates report AGB_ERR_RANK to the caller */
+                          * eigenvalue-guided eigenvector count fell short (AGB_D_NVEC = 0)
+                          * or whose eigenvectors overlap by more than 1e-2 after the
+                          * eigensolver (then with the cluster tolerance widened to 1e-3);
+                          * without it such gates report AGB_ERR_RANK / AGB_ERR_NOCONV */
 int agb_two_site_run(int dtype, int ngates, const int64_t* desc_dev, int64_t* desc_dev_out,
                      int max_chiL, int max_chiM, int max_chiR, int max_ell, void* ws, size_t ws_bytes,
                      void* stream, int flags);
 int agb_two_site_finalize(int dtype, int ngates, const int64_t* desc_dev, int max_chiL, int max_chiR,
                           int max_k, void* ws, void* stream);
+
+/* Singular values of every gate of the last agb_two_site_run on `ws` (read it
+ * before the workspace is reused): out[g * count + t] = sigma_t (double,
+ * descending) for the values the run computed, zero-padded to `count`.  The
+ * spectrum behind robust_svd's S (src/atlas_q/linalg_robust.py:37) as the
+ * reference's SVD-event records keep it (S_top128, src/atlas_q/tools_qih/tn_core.py:247-274). */
+int agb_two_site_spectra(int dtype, int ngates, const int64_t* desc_dev, const void* ws, int count, double* out,
+                         void* stream);
 
 /* (a6) Single-qubit gate, applied as the reference does: T'[a,t,b] = sum_s U[s,t] T[a,s,b]
  * (U^T; src/atlas_q/adaptive_mps.py:159-180).  In place. */
@@ -141,6 +156,13 @@ size_t agb_tune_tridiag_workspace(int dtype, int n, int count);
 int agb_tune_tridiag(int dtype, int n, int count, void* ws, size_t ws_bytes, void* stream, int* best_C,
                      float* best_ms);
 int agb_tuned_tridiag_cluster(int dtype, int n, int count);
+
+/* Tridiagonalisation used by the eigensolver: 0 the two-stage reduction
+ * (dense -> band of width 16 or 8 on a thread-block cluster, then bulge
+ * chasing in shared memory) wherever its buffers fit, else the one-stage
+ * kernel; 1 (default) the one-stage Householder kernel always.  Process-wide;
+ * this build's own switch (no reference counterpart), for comparing the paths. */
+int agb_set_tridiag_stages(int mode);
 
 /* Hermitian eigensolver (batched), exposed for robust_svd / tests.
  * Replaces the torch.linalg.svd call inside robust_svd (linalg_robust.py:37) when
@@ -192,6 +214,21 @@ int agb_mpo_mix(int dtype, const void* M, const void* W, void* N, int Lw, int Rw
  * The per-site einsum of expectation_value with a [1,2,2,1] MPO tensor
  * (src/atlas_q/mpo_ops.py:1145), batched over the observables of a sweep. */
 int agb_site_mix(int dtype, const void* M, const void* W, void* N, int count, int chiA, int chiB, void* stream);
+/* (f4) One site of apply_mpo_to_mps (src/atlas_q/mpo_ops.py:1034-1082, the
+ * einsum "lstr, atb -> lasrb" at :1068): out[(l, a), s, (r, b)] =
+ * sum_t W[l, s, t, r] A[a, t, b]; W [Dl, 2, 2, Dr] and A [chiA, 2, chiB] of the
+ * same dtype, out [Dl * chiA, 2, Dr * chiB].  Also the site product of the
+ * Pauli-exponential MPO (mpo_ops.py:1296-1358). */
+int agb_mpo_apply_site(int dtype, const void* W, const void* A, void* out, int Dl, int Dr, int chiA, int chiB,
+                       void* stream);
+/* (f1) TDVP local step with the index pattern of tdvp_apply_local_H_optimized
+ * (src/triton_kernels/tdvp_mpo_ops.py:89-106, einsum 'qli, lstn, isj, unj -> itj'):
+ * H[i, t, j] = sum_{q,l,s,n,u} L[q, l, i] W[l, s, t, n] A[i, s, j] R[u, n, j]
+ * with L [chiQ, Dl, chiI], W [Dl, 2, 2, Dn], A [chiI, 2, chiJ], R [chiU, Dn, chiJ],
+ * H [chiI, 2, chiJ].  ws: agb_tdvp_local_h_workspace bytes. */
+size_t agb_tdvp_local_h_workspace(int dtype, int Dl, int Dn, int chiI, int chiJ);
+int agb_tdvp_local_h(int dtype, const void* L, const void* W, const void* A, const void* R, void* H, int chiQ,
+                     int Dl, int chiI, int Dn, int chiU, int chiJ, void* ws, size_t ws_bytes, void* stream);
 /* out2[0] + i out2[1] = sum_{r,c} E[r,c] Q[c,r]  (double accuracy; out2 is device memory). */
 int agb_trace_prod(int dtype, const void* E, const void* Q, int n, double* out2, void* stream);
 
@@ -218,12 +255,15 @@ int agb_prof_end(double* ms_per_stage, int* marks_per_stage, int nstages);
  * reads singular values after the SVD; this one predicts the kept rank before
  * it from (chi_L, chi_R, entangling power, neighbouring-bond entropy, previous
  * rank).  X: [B][5] features, Y/T: [B] rank fraction in (0, 1).
- * agb_mlp_backward zeroes `grads` and accumulates d mean((y-t)^2) / d params;
- * loss_sum (optional) receives sum (y-t)^2.  agb_mlp_adam is AdamW (step >= 1). */
+ * agb_mlp_backward writes d mean((y-t)^2) / d params to `grads` and, if
+ * loss_sum is not NULL, sum (y-t)^2 to *loss_sum; deterministic (fixed-order
+ * reductions through ws, agb_mlp_backward_workspace(B) bytes).  agb_mlp_adam
+ * is AdamW (step >= 1). */
 #define AGB_MLP_NPARAM 8769
 int agb_mlp_forward(const float* params, const float* X, int B, float* Y, void* stream);
+size_t agb_mlp_backward_workspace(int B);
 int agb_mlp_backward(const float* params, const float* X, const float* T, int B, float* grads, float* loss_sum,
-                     void* stream);
+                     void* ws, size_t ws_bytes, void* stream);
 int agb_mlp_adam(float* params, const float* grads, float* m, float* v, int step, float lr, float beta1,
                  float beta2, float eps, float weight_decay, void* stream);
 
@@ -248,7 +288,8 @@ int agb_cgemm_tc_async(char opA, char opB, int batch, int M, int N, int K, const
                        size_t ws_bytes, int* status_dev, void* stream);
 
 /* Batched complex GEMM (SIMT reference-free kernel, used by the host layer):
- * C[b] = alpha * op(A[b]) op(B[b]) + beta * C[b]; op: 'N','T','C'. */
+ * C[b] = alpha * op(A[b]) op(B[b]) + beta * C[b]; op: 'N' (as stored), 'T' (transposed),
+ * 'C' (conjugate-transposed), 'R' (conjugated, not transposed). */
 int agb_cgemm_batched(int dtype, char opA, char opB, int batch, int M, int N, int K,
                       const void* A, int64_t lda, int64_t strideA, const void* B, int64_t ldb,
                       int64_t strideB, void* C, int64_t ldc, int64_t strideC, double alpha_re,

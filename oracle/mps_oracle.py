@@ -307,17 +307,59 @@ def expectation_product(tensors, ops):
     for i, A in enumerate(tensors):
         A = np.asarray(A, dtype=np.complex128)
         W = np.asarray(ops.get(i, np.eye(2)), dtype=np.complex128)
-        E = np.einsum("ab,atr,st,bsB->rB", E, A.conj(), W, A)
-        N = np.einsum("ab,asr,bsB->rB", N, A.conj(), A)
+        E = _env_step(E, A, W)
+        N = _env_step(N, A, None)
     return complex(E[0, 0] / N[0, 0])
+
+
+def _env_step(E, A, W):
+    """E'[r, B] = sum conj(A[a, t, r]) W[s, t] E[a, b] A[b, s, B] (the reference's
+    per-site einsum with a [1, 2, 2, 1] MPO tensor; W = None is the identity)."""
+    la, _, ra = A.shape
+    M = (E @ A.reshape(la, -1)).reshape(E.shape[0], 2, ra)       # [a, s, B]
+    if W is not None:
+        M = np.einsum("st,asB->atB", W, M)                        # ket s -> bra t
+    return A.reshape(la * 2, ra).conj().T @ M.reshape(la * 2, ra)
+
+
+def local_expectations(tensors, observables):
+    """<psi| prod_i O_i^T |psi> / <psi|psi> for product observables (site -> 2x2)
+    with the reference's convention (expectation_product), evaluated from left
+    and right identity environments: each observable costs the sites of its
+    support instead of a whole sweep (same contractions, other association)."""
+    ts = [np.asarray(t, dtype=np.complex128) for t in tensors]
+    n = len(ts)
+    Lenv = [np.ones((1, 1), dtype=np.complex128)]
+    for A in ts:
+        Lenv.append(_env_step(Lenv[-1], A, None))
+    Renv = [None] * (n + 1)
+    Renv[n] = np.ones((1, 1), dtype=np.complex128)
+    for i in range(n - 1, -1, -1):
+        A = ts[i]
+        la, _, ra = A.shape
+        X = (A.reshape(la * 2, ra) @ Renv[i + 1]).reshape(la, 2 * ra)   # [(b, s), r'] -> [b, (s, r')]
+        Renv[i] = X @ A.reshape(la, 2 * ra).conj().T                    # [ket b, bra a]
+    norm = complex(np.trace(Lenv[n] @ Renv[n]))
+    out = []
+    for obs in observables:
+        sites = sorted(obs)
+        E = Lenv[sites[0]]
+        for i in range(sites[0], sites[-1] + 1):
+            E = _env_step(E, ts[i], np.asarray(obs[i], np.complex128) if i in obs else None)
+        out.append(complex(np.trace(E @ Renv[sites[-1] + 1])) / norm)
+    return out
 
 
 def mps_overlap(ta, tb):
     """<a|b> for two MPS given as tensor lists."""
     E = np.ones((1, 1), dtype=np.complex128)
     for A, B in zip(ta, tb):
-        E = np.einsum("ab,asr,bsB->rB", E, np.asarray(A, np.complex128).conj(),
-                      np.asarray(B, np.complex128))
+        A = np.asarray(A, np.complex128)
+        B = np.asarray(B, np.complex128)
+        la, _, ra = A.shape
+        lb, _, rb = B.shape
+        T = (E @ B.reshape(lb, 2 * rb)).reshape(la * 2, rb)   # sum_b E[a,b] B[b,s,B]
+        E = A.reshape(la * 2, ra).conj().T @ T                 # sum_{a,s} conj(A[a,s,r]) T[a,s,B]
     return complex(E[0, 0])
 
 

@@ -216,6 +216,125 @@ def canonical_record():
     print("canonical written")
 
 
+def mpo_record():
+    """apply_mpo_to_mps and apply_pauli_exp_to_mps (src/atlas_q/mpo_ops.py:1034-1082,
+    1296-1358) and the three TDVP contractions of
+    src/triton_kernels/tdvp_mpo_ops.py:38-106, run by the reference on seeded
+    inputs.  The Pauli cases include strings of length >= 3, where the
+    reference's two-rail MPO drops the letters from the third site on."""
+    from atlas_q.mpo_ops import apply_mpo_to_mps, apply_pauli_exp_to_mps
+    import triton_kernels.tdvp_mpo_ops as tdo
+    out = {}
+    n = 6
+    ops = haar_brickwork(n, 4, seed=314)
+    mps, _ = run_ref(ops, n, 8, 1e-10, dtype=torch.complex128)
+    out["mpo_in_shapes"], out["mpo_in_flat"] = pack_tensors(mps.tensors)
+    Zo = torch.tensor([[1, 0], [0, -1]], dtype=torch.complex128)
+    Xo = torch.tensor([[0, 1], [1, 0]], dtype=torch.complex128)
+    Yo = torch.tensor([[0, -1j], [1j, 0]], dtype=torch.complex128)
+    H = MPOBuilder.sum_local_operators(n, [(i, Zo) for i in range(n)] + [(2, Yo)], device="cpu",
+                                       dtype=torch.complex128)
+    res = apply_mpo_to_mps(H, mps)
+    out["mpo_sum_state"] = res.to_statevector().numpy()
+    P = MPOBuilder.local_operator(Yo, 3, n, device="cpu", dtype=torch.complex128)
+    out["mpo_local_state"] = apply_mpo_to_mps(P, mps).to_statevector().numpy()
+    strings = ["XY", "ZX", "XYZ", "ZXXY"]
+    for k, ps in enumerate(strings):
+        m = AdaptiveMPS(len(ps), bond_dim=1, device="cpu", dtype=torch.complex128,
+                        dtype_policy=DTypePolicy(default=torch.complex128))
+        Hd = torch.tensor([[1, 1], [1, -1]], dtype=torch.complex128) / np.sqrt(2)
+        for q in range(len(ps)):
+            m.apply_single_qubit_gate(q, Hd)
+        m.apply_two_site_gate(0, haar_brickwork(2, 1, seed=9 + k)[0][2].to(torch.complex128))
+        out[f"pauli{k}_in"] = m.to_statevector().numpy()
+        apply_pauli_exp_to_mps(m, ps, 1j * 0.5, 0.6)
+        out[f"pauli{k}_out"] = m.to_statevector().numpy()
+    out["pauli_strings"] = np.array(strings)
+    g = torch.Generator().manual_seed(2718)
+
+    def cr(*shape):
+        return torch.complex(torch.randn(*shape, generator=g, dtype=torch.float64),
+                             torch.randn(*shape, generator=g, dtype=torch.float64))
+    L, A, W, R = cr(7, 3, 5), cr(5, 2, 6), cr(3, 2, 2, 4), cr(6, 4, 6)
+    out["tdvp_L"], out["tdvp_A"], out["tdvp_W"], out["tdvp_R"] = (t.numpy() for t in (L, A, W, R))
+    out["tdvp_left"] = tdo.tdvp_left_environment_init_optimized(cr(5, 3, 5) * 0 + L[:5], A, W).numpy()
+    out["tdvp_left_in"] = L[:5].numpy()
+    out["tdvp_right"] = tdo.tdvp_right_environment_init_optimized(R, A, W).numpy()
+    out["tdvp_local"] = tdo.tdvp_apply_local_H_optimized(L, W, A, R).numpy()
+    np.savez_compressed(os.path.join(HERE, "mpo_apply.npz"), **out)
+    print("mpo / pauli / tdvp written")
+
+
+def qiskit_record():
+    """The reference backend's MPS route (ATLASQBackend._run_mps,
+    src/atlas_q/adapters/qiskit_adapter.py:383-404) on tests/qiskit_like.py's
+    six-qubit circuit: its statevector (the counts are torch.multinomial
+    draws and are compared by distribution only)."""
+    import warnings
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    from qiskit_like import sample_circuit
+    import importlib.util
+    # the adapters package also imports its Cirq adapter, which needs Cirq;
+    # load the Qiskit adapter's module file on its own
+    spec = importlib.util.spec_from_file_location(
+        "qiskit_adapter_ref", os.path.join(REF, "src", "atlas_q", "adapters", "qiskit_adapter.py"))
+    qa = importlib.util.module_from_spec(spec)
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        spec.loader.exec_module(qa)
+    fake = types.SimpleNamespace(_max_bond_dim=128)
+    fake._apply_gate_to_mps = lambda mps, name, qubits, params: qa.ATLASQBackend._apply_gate_to_mps(
+        fake, mps, name, qubits, params)
+    fake._samples_to_counts = lambda samples, n=None: qa.ATLASQBackend._samples_to_counts(fake, samples, n)
+    angle = lambda v: torch.tensor(v, dtype=torch.float64)  # noqa: E731
+    counts, sv = qa.ATLASQBackend._run_mps(fake, sample_circuit(angle), 4000, 7)
+    np.savez_compressed(os.path.join(HERE, "qiskit_mps.npz"), statevector=sv.numpy(), shots=4000,
+                        count_keys=np.array(sorted(counts)), count_vals=np.array([counts[k] for k in sorted(counts)]))
+    print("qiskit route written")
+
+
+def headline_record(seeds=(1234, 1235, 1236), pinned=150, checkpoints=(150, 250, 330, 390)):
+    """The 40-qubit Haar brickwork (depth 20, chi_max 256, eps 1e-8) through the
+    reference in complex64 and in complex128, gate by gate in lockstep.  Kept:
+    for the first seed, the per-gate kept singular values (complex64) and logs
+    of the first `pinned` gates, and the kept ranks of every gate in both
+    precisions; for every seed, the complex64-vs-complex128 fidelity at the
+    checkpoints (the reference's own float32 drift once the chi cap binds)."""
+    from oracle import mps_oracle as mo
+    out = {"seeds": np.array(seeds), "checkpoints": np.array(checkpoints)}
+    fids = np.zeros((len(seeds), len(checkpoints)))
+    for si, seed in enumerate(seeds):
+        ops = haar_brickwork(40, 20, seed=seed)
+        runs = {}
+        for dt in (torch.complex64, torch.complex128):
+            runs[dt] = AdaptiveMPS(40, bond_dim=1, eps_bond=1e-8, chi_max_per_bond=256, device="cpu", dtype=dt,
+                                   dtype_policy=DTypePolicy(default=dt))
+        spectra = []
+        for g, (_, q, U) in enumerate(ops):
+            _REC.clear()
+            runs[torch.complex64].apply_two_site_gate(q, U.to(torch.complex64))
+            if g < pinned:
+                spectra.append(_REC[-1].astype(np.float32))
+            runs[torch.complex128].apply_two_site_gate(q, U.to(torch.complex128))
+            if g + 1 in checkpoints:
+                a = [t.numpy() for t in runs[torch.complex64].tensors]
+                b = [t.numpy() for t in runs[torch.complex128].tensors]
+                fids[si, list(checkpoints).index(g + 1)] = mo.mps_fidelity(a, b)
+        print("headline seed", seed, "fidelity c64 vs c128 at", list(checkpoints), fids[si])
+        if si == 0:
+            l64 = runs[torch.complex64].statistics.logs
+            k = [int(x) for x in l64["k_star"]]
+            out["k64"] = np.array(k, dtype=np.int64)
+            out["k128"] = np.array(runs[torch.complex128].statistics.logs["k_star"], dtype=np.int64)
+            kept = [sp[:kk] for sp, kk in zip(spectra, k[:pinned])]
+            out["sv_lens"], out["sv_flat"] = pack_spectra(kept)
+            for key in ("eps_local", "entropy", "condS"):
+                out["log_" + key] = np.array(l64[key][:pinned], dtype=np.float64)
+    out["fid_c64_c128"] = fids
+    np.savez_compressed(os.path.join(HERE, "brickwork_n40_d20_chi256.npz"), n=40, chi=256, eps=1e-8,
+                        depth=20, pinned=pinned, **out)
+
+
 if __name__ == "__main__":
     choose_rank_cases()
     known_answers()
@@ -225,3 +344,6 @@ if __name__ == "__main__":
     circuit_record("hea_n10_l3_chi16", hea_circuit(10, 3, seed=3), 10, 16, 1e-8)
     expectations_record()
     canonical_record()
+    mpo_record()
+    qiskit_record()
+    headline_record()

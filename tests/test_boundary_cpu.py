@@ -150,3 +150,60 @@ def test_new_entry_points_validate_arguments_without_a_gpu(lib):
                                   1.0, 0.0, 0.0, 0.0, P, 0, P, P) == _lib.AGB_ERR_ARG
     # no launch has failed in this process
     assert lib.agb_last_error() == b""
+
+
+def test_samples_to_counts_formats_like_the_reference():
+    """adapters.samples_to_counts: format(sample, '0{n}b') keys (qubit 0 leftmost)."""
+    from atlasq_gb300.adapters import samples_to_counts
+    c = samples_to_counts(np.array([0, 5, 5, 7]), 3)
+    assert c == {"000": 1, "101": 2, "111": 1}
+    assert samples_to_counts({"01": 3}) == {"01": 3}
+    assert samples_to_counts([2, 2], None) == {"10": 2}
+
+
+def test_svd_event_log_roundtrip(tmp_path, monkeypatch):
+    """svd_log writes the reference's record fields (tools_qih/tn_core.py:247-274)
+    to svd_events_*.jsonl.gz under $QIH_SVD_LOG_DIR, and read_events reads them."""
+    from atlasq_gb300 import svd_log
+    monkeypatch.setenv("QIH_SVD_LOG_DIR", str(tmp_path))
+    lg = svd_log.get_logger()
+    lg.spectrum(bond=3, pre_rank=16, chi_max=32, tol=1e-8, total_weight=2.0, sigma=[1.0, 0.5, 0.25], keep=2,
+                step=7, chi_left=8, chi_right=16, features=[0.1, 0.2, 0.3, 0.4, 0.5], full=16)
+    lg.close()
+    recs = list(svd_log.read_events(str(tmp_path)))
+    assert len(recs) == 1
+    r = recs[0]
+    for key in ("host", "pid", "run_ts", "kind", "i", "j", "pre_rank", "chi_max", "tol", "adaptive", "entangler",
+                "total_weight", "S_top128", "adaptive_keep"):
+        assert key in r
+    assert r["kind"] == "svd_spectrum" and r["i"] == 3 and r["j"] == 4 and r["adaptive_keep"] == 2
+    assert len(r["S_top128"]) == 128 and r["S_top128"][:3] == [1.0, 0.5, 0.25] and r["S_top128"][3] == 0.0
+    assert r["features"] == [0.1, 0.2, 0.3, 0.4, 0.5] and r["full"] == 16
+    monkeypatch.delenv("QIH_SVD_LOG_DIR")
+    assert svd_log.get_logger() is None
+
+
+def test_pauli_fixture_records_the_reference_deviation():
+    """The reference's exp(i lam P) is exact for Pauli strings of length <= 2 and
+    not for longer ones (tests/golden/mpo_apply.npz); the package's MPO builder
+    (pauli_exp_mpo, CPU tensors) contracts to the exact operator for all."""
+    import torch
+    from atlasq_gb300.mpo_ops import pauli_exp_mpo
+    g = load_golden("mpo_apply")
+    P = {"I": np.eye(2), "X": np.array([[0, 1], [1, 0]]), "Y": np.array([[0, -1j], [1j, 0]]), "Z": np.diag([1., -1.])}
+    lam = 0.3
+    for k, ps in enumerate(str(x) for x in g["pauli_strings"]):
+        Pm = np.array([[1.0]])
+        for c in ps:
+            Pm = np.kron(Pm, P[c])
+        op = np.cos(lam) * np.eye(2 ** len(ps)) + 1j * np.sin(lam) * Pm
+        exact = op @ g[f"pauli{k}_in"]
+        f = abs(np.vdot(exact, g[f"pauli{k}_out"])) ** 2
+        assert (f > 1 - 1e-10) == (len(ps) <= 2), (ps, f)
+        mpo = pauli_exp_mpo(ps, lam, device="cpu", dtype=torch.complex128)
+        T = None
+        for W in mpo.tensors:
+            T = W if T is None else torch.einsum("...a,astr->...str", T, W)
+        n = len(ps)
+        T = T.reshape([2] * (2 * n)).permute([2 * i for i in range(n)] + [2 * i + 1 for i in range(n)])
+        assert np.allclose(T.reshape(2 ** n, 2 ** n).numpy(), op, atol=1e-12)

@@ -30,3 +30,34 @@ def test_model_eigenvalues_and_separated_leading_group():
         Y = np.stack([fm.inverse_iteration(d, e, lam[t], rng) for t in range(10)], axis=1).astype(np.float64)
         assert np.linalg.svd(Y, compute_uv=False).min() > 0.9
         assert np.max(np.abs(Y.T @ Y - np.eye(10))) < 0.1
+
+
+def _sturm_count_late_replacement(d, e, x):
+    """The former kernel order: a pivot is counted first and replaced by
+    -pivmin only when the next step divides by it."""
+    x = np.float32(x)
+    q = d[0] - x
+    c = int(q < 0)
+    for k in range(1, len(d)):
+        if abs(q) < np.float32(1e-30):
+            q = np.float32(-1e-30)
+        q = d[k] - x - (e[k - 1] * e[k - 1]) / q
+        c += int(q < 0)
+    return c
+
+
+def test_sturm_count_with_a_pivot_that_cancels_to_zero():
+    """T - 2I has a leading 2 x 2 block that is exactly singular in float32
+    (pivots 1, then 0.5625 - 0.5625 = 0).  Counting that zero pivot before
+    replacing it by -pivmin (the kernel's order, LAPACK dlaebz's) gives the
+    exact count of eigenvalues below 2; counting it as non-negative and
+    replacing it only at the next division loses one.  That lost count made
+    the bisection return a leading eigenvalue midway between two neighbours
+    1.6e-5 apart, and inverse iteration then produced overlapping vectors."""
+    d = np.array([3.0, 2.5625, 2.0], dtype=np.float32)
+    e = np.array([0.75, 0.5, 0.0], dtype=np.float32)
+    T = np.diag(d.astype(np.float64)) + np.diag(e[:2].astype(np.float64), 1) + np.diag(e[:2].astype(np.float64), -1)
+    exact = int(np.sum(np.linalg.eigvalsh(T) < 2.0))
+    assert exact == 1
+    assert fm._sturm(d, e, 2.0) == exact
+    assert _sturm_count_late_replacement(d, e, 2.0) == exact - 1

@@ -84,6 +84,20 @@ def test_mlp_backward_matches_oracle(B):
 
 
 @pytest.mark.gpu
+def test_mlp_training_is_deterministic():
+    """The gradient reductions run in a fixed order (no float atomics): two
+    trainings from the same start on the same minibatches end bit-identical."""
+    from atlasq_gb300.rank_predictor import RankPredictor
+    X, T = _batch(11, 3000)
+    outs = []
+    for _ in range(2):
+        rp = RankPredictor(seed=3)
+        rp.train(X, T, steps=60, batch=1000, lr=3e-3)
+        outs.append(rp.params.cpu().numpy().copy())
+    assert np.array_equal(outs[0], outs[1])
+
+
+@pytest.mark.gpu
 def test_mlp_adam_matches_oracle():
     from atlasq_gb300 import _lib
     from atlasq_gb300._lib import check, ptr, stream_ptr
