@@ -577,14 +577,18 @@ def apply_gate_entries(entries):
             res[g] = r
             entries[g][0].rank_fallbacks += 1
             entries[g][0].ell_total += r["ell"]
-    # precision promotion (adaptive_mps.py:268-274)
+    # precision promotion (adaptive_mps.py:268-274), and the robust-SVD
+    # fallback (linalg_robust.py:17-52 retries a failed factorisation at
+    # higher precision): a complex64 gate whose eigenvectors still failed the
+    # orthogonality guard after the device repair is re-run in complex128
     promote = [g for g, r in enumerate(res)
-               if math.isfinite(r["condS"]) and r["condS"] > entries[g][0].dtype_policy.promote_if_cond_gt
-               and dt != _C128]
+               if dt != _C128 and (r["status"] == _lib.AGB_ERR_NOCONV or (
+                   math.isfinite(r["condS"]) and r["condS"] > entries[g][0].dtype_policy.promote_if_cond_gt))]
     if promote:
         r2 = _run_pipeline([entries[g] for g in promote], _C128, None, all_vectors=True, spectra=spectra)
         for g, r in zip(promote, r2):
-            r["driver"] = "gb300_gram_heevd_c128"
+            r["driver"] = ("gb300_gram_heevd_c128_robust" if res[g]["status"] == _lib.AGB_ERR_NOCONV
+                           else "gb300_gram_heevd_c128")
             res[g] = r
     elapsed = (time.perf_counter() - t0) * 1000.0 / len(entries)
     for m, idx in groups.values():
@@ -714,7 +718,7 @@ def _run_pipeline(entries, dt, ells, all_vectors=False, cluster_tol=None, spectr
         if sig is not None:
             row_s = sig[g]
             r["sigma"] = row_s[:int(np.count_nonzero(row_s))].copy()
-        if st not in (_lib.AGB_OK, _lib.AGB_ERR_RANK):
+        if st not in (_lib.AGB_OK, _lib.AGB_ERR_RANK) and not (st == _lib.AGB_ERR_NOCONV and dt != _C128):
             check(st, f"two-site update on bond {i}")
         ok = m._budget_ok_fn(chiL, chiM, chiR, dt)
         if ok is not None and st == _lib.AGB_OK:

@@ -353,7 +353,7 @@ __global__ void __launch_bounds__(128) invit_kernel(const HeevdProb* __restrict_
     // loads its operands into registers first and then runs the serial chain:
     // IB loads in flight instead of one dependent load per step.  Within a
     // chunk every load of Y precedes the store to the same element.
-    constexpr int IB = 8;
+    constexpr int IB = 16;
     R bi = Y[t] * s;
     for (int i0 = 0; i0 < n - 1; i0 += IB) {
       R yb[IB], pv[IB], lm[IB];
@@ -477,35 +477,6 @@ AGB_DEV void tri_lu(const R* d, const R* e, int n, R lam, R piv, R* U0, R* U1, R
   U2[(int64_t)(n - 1) * L + t] = 0;
 }
 
-// In place: y <- (T - lam I)^{-1} y using the stored factors; returns ||y||^2.
-template <typename R>
-AGB_DEV R tri_solve(R* Y, int n, const R* U0, const R* U1, const R* U2, const R* Lm, const R* Pv,
-                    int64_t L, int t, R piv) {
-  R bi = Y[t];
-  for (int i = 0; i < n - 1; ++i) {
-    R bn = Y[(i + 1) * L + t];
-    if (Pv[i * L + t] != R(0)) {
-      const R tmp = bi;
-      bi = bn;
-      bn = tmp;
-    }
-    Y[i * L + t] = bi;
-    bi = bn - Lm[i * L + t] * bi;
-  }
-  Y[(int64_t)(n - 1) * L + t] = bi;
-  R x1 = 0, x2 = 0, nrm = 0;
-  for (int i = n - 1; i >= 0; --i) {
-    R u = U0[i * L + t];
-    if (fabs(u) < piv) u = copysign(piv, u == R(0) ? R(1) : u);
-    const R x = (Y[i * L + t] - U1[i * L + t] * x1 - U2[i * L + t] * x2) / u;
-    Y[i * L + t] = x;
-    nrm += x * x;
-    x2 = x1;
-    x1 = x;
-  }
-  return nrm;
-}
-
 // y <- (T - lam I)^{-1} (s * y) for column t of Y (stride L) with the stored
 // factors of column t; returns ||y||^2.  Factor and iterate loads do not depend
 // on the recurrence, so each chunk of IB steps loads them into registers first
@@ -513,7 +484,7 @@ AGB_DEV R tri_solve(R* Y, int n, const R* U0, const R* U1, const R* U2, const R*
 template <typename R>
 AGB_DEV R tri_solve_pf(R* Y, int n, const R* U0, const R* U1, const R* U2, const R* Lm, const R* Pv, int64_t L,
                        int t, R piv, R s) {
-  constexpr int IB = 8;
+  constexpr int IB = 16;
   R bi = Y[t] * s;
   for (int i0 = 0; i0 < n - 1; i0 += IB) {
     R yb[IB], pv[IB], lm[IB];
@@ -859,7 +830,8 @@ __global__ void __launch_bounds__(256) cluster_invit_kernel(const HeevdProb* __r
     prev = s_shift;
     for (int it = 0; it < 2; ++it) {
       cgs2_normalize(ycol, Y, n, L, t0, j, coef, red, part);
-      if (tid == 0) s_nrm = tri_solve(ycol, n, f, f + n, f + 2 * n, f + 3 * n, f + 4 * n, 1, 0, piv);
+      // (the prefetching solve with unit scale: the same operations as tri_solve)
+      if (tid == 0) s_nrm = tri_solve_pf(ycol, n, f, f + n, f + 2 * n, f + 3 * n, f + 4 * n, 1, 0, piv, R(1));
       __syncthreads();
       if (!(s_nrm < R(1e300)) || !(s_nrm > R(0))) {
         for (int r = tid; r < n; r += nt)

@@ -20,15 +20,20 @@
 // (re-orthogonalised inverse iteration, LAPACK stein's scheme); wider gaps
 // leave inverse-iteration vectors within ~(bisection error / gap)^3 of
 // orthogonal, far below what the Newton-Schulz polish removes.  A problem whose
-// first polish product V^H V still shows an overlap above kOrthGuard (two
-// polish steps reach float32 orthonormality only from overlaps below ~1e-2)
-// has its vector phase re-run with the wider kClusterTolWide (the repair pass
-// of the two-site pipeline).  On dense spectra of large Gram matrices
-// (n >= 512) the wide tolerance chains hundreds of eigenvalues into one
-// cluster, so it is only a repair setting.
+// first polish product V^H V still shows an overlap above kOrthGuard has its
+// vector phase re-run with the wider kClusterTolWide (the repair pass of the
+// two-site pipeline).  The guard separates two measured populations: two
+// inverse-iteration vectors converged onto one eigenvector (the zero-pivot
+// Sturm defect) overlap by 0.48-0.56 and leave a direction missing, while
+// imprecise vectors of a near-degenerate group (64-qubit HEA gates, chi 512)
+// overlap by up to 0.022 and span the right subspace.  Two Newton-Schulz steps
+// take an overlap d to ~0.42 d^4 (3e-6 from 0.05), so everything below the
+// guard is polished to float32 orthonormality.  On dense spectra of large Gram
+// matrices (n >= 512) the wide tolerance chains hundreds of eigenvalues into
+// one cluster, so it is only a repair setting.
 constexpr double kClusterTol = 1e-5;
 constexpr double kClusterTolWide = 1e-3;
-constexpr float kOrthGuard = 1e-2f;
+constexpr float kOrthGuard = 5e-2f;
 AGB_HD bool orth_exceeds(unsigned max2_bits) {
   union {
     unsigned u;

@@ -174,3 +174,125 @@ def collect_training_data(circuit_fn, seeds, n, chi, eps, device="cuda"):
             Xs.append(feat)
             Ts.append(k / max(full, 1))
     return np.asarray(Xs, dtype=np.float32), np.asarray(Ts, dtype=np.float32)
+
+
+# ---------------------------------------------------------------------- training pipeline
+# Plain runs log one SVD event per gate (svd_log.py, the reference's record with
+# the predictor's features added); training reads the events back, so the
+# pipeline is: log_plain_runs -> training_data_from_events -> RankPredictor.train
+# -> save_predictor.  The reference trains its predictor from the same event
+# stream (scripts/ai_tools/finetune_rank_predictor.py over svd_logger files).
+
+def log_plain_runs(circuit_fn, seeds, n, chi, eps, log_dir, device="cuda"):
+    """Run the plain simulator (no predictor) on ``circuit_fn(seed)`` for every
+    seed with the SVD-event log on; returns the log file's path."""
+    from . import svd_log
+    from .adaptive_mps import AdaptiveMPS
+    logger = svd_log.SVDEventLogger(log_dir)
+    try:
+        for sd in seeds:
+            m = AdaptiveMPS(n, bond_dim=1, eps_bond=eps, chi_max_per_bond=chi, device=device)
+            m.feature_log = []   # features computed per gate -> written into the events
+            m.svd_logger = logger
+            for kind, q, U in circuit_fn(sd):
+                if kind == "2q":
+                    m.apply_two_site_gate(q, U)
+                else:
+                    m.apply_single_qubit_gate(q, U)
+            m.flush()
+    finally:
+        logger.close()
+    return str(logger.path)
+
+
+def training_data_from_events(events):
+    """(features [N, 5] float32, kept-rank fraction [N] float32) from SVD events
+    that carry ``features`` and ``full`` (records without them are skipped)."""
+    Xs, Ts = [], []
+    for rec in events:
+        if "features" not in rec or "full" not in rec:
+            continue
+        Xs.append(rec["features"])
+        Ts.append(rec["adaptive_keep"] / max(int(rec["full"]), 1))
+    return np.asarray(Xs, dtype=np.float32).reshape(-1, 5), np.asarray(Ts, dtype=np.float32)
+
+
+def default_predictor_path(name="hea64"):
+    """Weights shipped with the package: ``hea64`` trained on plain runs of the
+    64-qubit hardware-efficient ansatz (12 layers, chi_max 512, eps 1e-8);
+    ``brickwork40`` on plain runs of the 40-qubit Haar brickwork (depth 20,
+    chi_max 256, eps 1e-8, seeds disjoint from the benchmark's)."""
+    import os
+    return os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", f"rank_predictor_{name}.npz")
+
+
+def save_predictor(pred, path, **meta):
+    import json
+    np.savez(path, params=pred.params.detach().cpu().numpy(), margin=np.float64(pred.margin),
+             pad=np.int64(pred.pad), meta=np.array(json.dumps(meta)))
+
+
+def load_predictor(path=None, device="cuda"):
+    """A RankPredictor with saved weights (``default_predictor_path()`` when path is None)."""
+    d = np.load(path or default_predictor_path())
+    return RankPredictor(device=device, params=torch.from_numpy(d["params"]), margin=float(d["margin"]),
+                         pad=int(d["pad"]))
+
+
+def _main(argv=None):
+    """python -m atlasq_gb300.rank_predictor --runs R --log-dir DIR --out FILE [--circuit hea|brickwork]
+
+    Logs R seeded plain runs of the 64-qubit hardware-efficient ansatz (12
+    layers of RY RZ on every qubit then a CZ ladder, chi_max 512, eps 1e-8;
+    ``--circuit brickwork``: the 40-qubit Haar brickwork, depth 20, chi_max
+    256), trains the MLP on the GPU on the logged (features, kept rank) pairs
+    and saves the weights.  Prints one JSON summary line."""
+    import argparse
+    import json
+    import time
+    from .circuits import haar_brickwork, hea_circuit
+    from . import svd_log
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--circuit", default="hea", choices=["hea", "brickwork"])
+    ap.add_argument("--runs", type=int, default=16)
+    ap.add_argument("--first-seed", type=int, default=1000)
+    ap.add_argument("--qubits", type=int, default=None, help="64 (hea) / 40 (brickwork)")
+    ap.add_argument("--layers", type=int, default=None, help="12 (hea) / depth 20 (brickwork)")
+    ap.add_argument("--chi", type=int, default=None, help="512 (hea) / 256 (brickwork)")
+    ap.add_argument("--eps", type=float, default=1e-8)
+    ap.add_argument("--steps", type=int, default=1500)
+    ap.add_argument("--log-dir", required=True)
+    ap.add_argument("--out", required=True)
+    ap.add_argument("--device", default="cuda")
+    a = ap.parse_args(argv)
+    hea = a.circuit == "hea"
+    a.qubits = a.qubits or (64 if hea else 40)
+    a.layers = a.layers or (12 if hea else 20)
+    a.chi = a.chi or (512 if hea else 256)
+    t0 = time.perf_counter()
+    seeds = list(range(a.first_seed, a.first_seed + a.runs))
+    circ = ((lambda sd: hea_circuit(a.qubits, a.layers, seed=sd)) if hea else
+            (lambda sd: haar_brickwork(a.qubits, a.layers, seed=sd)))
+    path = log_plain_runs(circ, seeds, a.qubits, a.chi, a.eps, a.log_dir, device=a.device)
+    t_log = time.perf_counter() - t0
+    X, T = training_data_from_events(svd_log.read_events(path))
+    rng = np.random.default_rng(0)
+    perm = rng.permutation(len(T))
+    nval = max(1, len(T) // 10)
+    val, tr = perm[:nval], perm[nval:]
+    pred = RankPredictor(device=a.device, seed=0)
+    t1 = time.perf_counter()
+    hist = pred.train(X[tr], T[tr], steps=a.steps)
+    t_train = time.perf_counter() - t1
+    fv = pred.predict_fraction(X[val]).cpu().numpy()
+    save_predictor(pred, a.out, circuit=a.circuit, runs=a.runs, first_seed=a.first_seed, qubits=a.qubits,
+                   layers=a.layers,
+                   chi=a.chi, eps=a.eps, samples=int(len(T)))
+    print(json.dumps({"samples": int(len(T)), "log": path, "log_seconds": t_log, "train_seconds": t_train,
+                      "final_loss": hist[-1], "val_mae_fraction": float(np.mean(np.abs(fv - T[val]))),
+                      "val_under_predicted": float(np.mean(fv * (1 + pred.margin) < T[val])),
+                      "out": a.out}), flush=True)
+
+
+if __name__ == "__main__":
+    _main()

@@ -17,6 +17,10 @@ Lines printed (rank 0, one JSON object):
            (PyTorch-CPU port with the reference's own library calls), bounded sample
   plain_gpu     the reference call sequence on this GPU with torch complex64
            contraction + torch.linalg.svd (cuSOLVER), for the plain-form comparison
+  learned  the host-synchronised pipeline with the learned rank predictor sizing
+           each gate's eigensolver (weights shipped in atlasq_gb300/data/)
+  fidelity_vs_fp64  |<psi|psi_fp64>|^2 of each arm's final state against this
+           package's complex128 run of the same circuit
 
 ``--impl reference`` times the CPU port of the reference path instead.
 Multi-GPU (torchrun): independent replicas per rank, no collective on the data
@@ -402,14 +406,20 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
-    ap.add_argument("--fp64-check", action="store_true", help="also run the complex128 GPU path and report fidelity")
     ap.add_argument("--resident", action="store_true",
                     help="AdaptiveMPS(device_resident=True), no host synchronisation between batches: the default")
     ap.add_argument("--host-sync", action="store_true",
                     help="run AdaptiveMPS(device_resident=False): ranks read back after every batch")
     ap.add_argument("--workload", default="brickwork40", choices=["brickwork40", "batch256", "sample50", "hea64"],
                     help="brickwork40 is the headline; the others are the secondary workloads")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-rank arm")
     args = ap.parse_args()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        # one process per GPU: relaunch this command under torch.distributed.run
+        cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={args.gpus}",
+               "--master-addr", "127.0.0.1", "--master-port", os.environ.get("MASTER_PORT", "29511"),
+               os.path.abspath(__file__)] + sys.argv[1:]
+        sys.exit(subprocess.call(cmd))
     global RESIDENT
     RESIDENT = not args.host_sync
     if args.workload != "brickwork40" and args.impl == "ours":
@@ -475,26 +485,27 @@ def main():
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         m = run_ours(ops_pinned, device)
-        res = m._tensors[-1].cpu()  # device->host read of the step's result
+        res = [t.cpu() for t in m.tensors]  # device->host read of the step's result: every site tensor
         torch.cuda.synchronize()
         e2e_ms += (time.perf_counter() - t0) * 1000.0
     e2e_ms = max_over_ranks(dist, e2e_ms, device) / args.steps
     # per step: gate matrices (16 complex64) + two descriptor uploads per gate (32 int64 each);
-    # back: one descriptor read per gate + the final site tensor
+    # back: one descriptor read per gate + every site tensor of the final state
     # host-synchronised: two descriptor uploads per gate (run, finalize), one read;
     # resident: one upload per gate, the descriptors read once at the end (statistics)
     h2d = ngates * 16 * 8 + ngates * (1 if RESIDENT else 2) * 32 * 8
-    d2h = ngates * 32 * 8 + res.numel() * res.element_size() + (4 * (N_QUBITS + 1) if RESIDENT else 0)
+    d2h = ngates * 32 * 8 + sum(t.numel() * t.element_size() for t in res) + (4 * (N_QUBITS + 1) if RESIDENT else 0)
     e2e = {"value": ngates * ws / (e2e_ms / 1000.0), "unit": "gates/s", "h2d_bytes_per_step": h2d,
            "d2h_bytes_per_step": d2h}
 
     # ---------------------------------------------------------------- the other execution mode (same timing)
     alt_ms = 0.0
+    alt = None
     for _ in range(args.steps):
         flush_buf.zero_()
         s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         s.record()
-        run_ours(ops_dev, device, resident=not RESIDENT)
+        alt = run_ours(ops_dev, device, resident=not RESIDENT)
         e.record()
         e.synchronize()
         alt_ms += s.elapsed_time(e)
@@ -552,14 +563,24 @@ def main():
     roof.update({"kernel": dom, "peak_source": src, "stage_ms_per_step": {k: round(v, 3) for k, v in stage_ms.items()},
                  "algorithmic_flops_per_step": wf, "algorithmic_bytes_per_step": wb})
     if dom == "tridiag":
-        # DRAM bytes of one launch from an ncu capture of this kernel on this
-        # workload: 20 Gram matrices of 512 x 512 (one saturated layer), read
-        # 14 264 064 B, written 0 B, against
-        # 20 x 2 n^2 x 8 B = 83 886 080 algorithmic bytes (the rest is served from L2,
-        # where the Gram GEMM left it)
+        # The Householder reduction keeps each matrix in the shared memory of an
+        # 8-CTA cluster, so HBM is not what limits it: one launch per layer runs
+        # n - 1 dependent column steps, each with two cluster barriers.  Its
+        # FP32 rate is reported beside the HBM fraction of the contract.
+        fp32_peak = 152 * 128 * 2 * (clocks.get("sm_max_mhz") or 2070.0) / 1e6  # TFLOP/s, SIMT FMA
+        roof["limiter"] = "latency: serial column chain with two cluster barriers per column (not HBM)"
+        roof["fp32_simt"] = {"achieved_tflops": wf / t_dom / 1e12 if t_dom > 0 else 0.0,
+                             "peak_tflops": fp32_peak,
+                             "frac": (wf / t_dom / 1e12) / fp32_peak if t_dom > 0 else 0.0}
+        # DRAM bytes of ONE launch (one saturated layer: 20 Gram matrices of
+        # 512 x 512) from an ncu capture of this kernel on this workload: read
+        # 14 264 064 B, written 0 B, against that launch's 20 x 2 n^2 x 8 B =
+        # 83 886 080 algorithmic bytes (the rest is served from L2, where the
+        # Gram GEMM left it).  Per launch, not per step.
         roof["traffic"] = 14264064
-        roof["traffic_launch"] = {"matrices": 20, "n": 512, "algorithmic_bytes": 20 * 2 * 512 * 512 * 8,
-                                  "source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch"}
+        roof["traffic_per_launch"] = {"matrices": 20, "n": 512, "algorithmic_bytes": 20 * 2 * 512 * 512 * 8,
+                                      "dram_bytes": 14264064,
+                                      "source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch"}
 
     line = {"metric": METRIC, "value": value, "unit": "gates/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
@@ -570,6 +591,21 @@ def main():
                        "execution": "device-resident (no host sync between batches)" if RESIDENT else
                                     "host-synchronised (ranks read back after every batch)"},
             "clocks": clocks, "gpu_launches": launches, "e2e": e2e, "roofline": roof, "other_mode": other_mode}
+
+    # ---------------------------------------------------------------- FP64 reference state
+    # this package's complex128 run (host-synchronised) of the same circuit
+    t0 = time.perf_counter()
+    m64 = run_ours(ops_dev, device, dtype=torch.complex128, resident=False)
+    torch.cuda.synchronize()
+    t64 = time.perf_counter() - t0
+    n64 = mps_overlap(m64.tensors, m64.tensors).real
+
+    def fid64(ts):
+        f = mps_overlap(ts, m64.tensors)
+        return abs(f) ** 2 / (mps_overlap(ts, ts).real * n64)
+
+    line["fidelity_vs_fp64"] = {"value": fid64(last.tensors), "fp64_gpu_seconds": t64,
+                                "what": "|<psi|psi_fp64>|^2 of the final state; psi_fp64 = this package's complex128 run"}
 
     # ---------------------------------------------------------------- plain form on the same GPU
     if not args.no_plain:
@@ -584,15 +620,41 @@ def main():
         fb = mps_overlap(pt, pt).real
         line["plain_gpu"] = {"value": ngates / tp, "unit": "gates/s",
                              "what": "reference call sequence on this GPU: torch complex64 einsum + torch.linalg.svd (cuSOLVER) + host rank rule",
-                             "fidelity_vs_ours": abs(f) ** 2 / (fa * fb)}
-    if args.fp64_check:
-        t0 = time.perf_counter()
-        m64 = run_ours(ops_dev, device, dtype=torch.complex128)
-        torch.cuda.synchronize()
-        f = mps_overlap(last.tensors, m64.tensors)
-        fa = mps_overlap(last.tensors, last.tensors).real
-        fb = mps_overlap(m64.tensors, m64.tensors).real
-        line["fidelity_vs_fp64"] = {"value": abs(f) ** 2 / (fa * fb), "fp64_gpu_seconds": time.perf_counter() - t0}
+                             "fidelity_vs_ours": abs(f) ** 2 / (fa * fb), "fidelity_vs_fp64": fid64(pt)}
+
+    # ---------------------------------------------------------------- learned-rank arm
+    from atlasq_gb300 import rank_predictor as rp
+    wpath = rp.default_predictor_path("brickwork40")
+    if not args.no_learned and os.path.exists(wpath):
+        pred = rp.load_predictor(wpath, device=device)
+
+        def run_learned():
+            m = aq.AdaptiveMPS(N_QUBITS, bond_dim=1, eps_bond=EPS, chi_max_per_bond=CHI, device=device)
+            m.rank_predictor = pred
+            for _, q, U in ops_dev:
+                m.apply_two_site_gate(q, U)
+            m.flush()
+            return m
+        run_learned()
+        lm_ms, ml = 0.0, None
+        for _ in range(args.steps):
+            flush_buf.zero_()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record()
+            ml = run_learned()
+            e.record()
+            e.synchronize()
+            lm_ms += s.elapsed_time(e)
+        lm_ms /= args.steps
+        plain_host = alt if RESIDENT else last
+        line["learned"] = {
+            "value": ngates / (lm_ms / 1000.0), "unit": "gates/s", "fidelity_vs_fp64": fid64(ml.tensors),
+            "execution": "host-synchronised; the MLP (agb_mlp_forward) sizes each gate's eigenpair count",
+            "predictor": ("5-64-64-64-1 MLP trained on the GPU on plain runs of the 40-qubit brickwork "
+                          "(depth 20, chi_max 256; seeds 2000-2015, disjoint from this circuit's)"),
+            "rank_fallbacks": ml.rank_fallbacks,
+            "eigenpairs_vs_plain_host": ml.ell_total / max(plain_host.ell_total, 1),
+            "same_bond_dims_as_plain_host": list(ml.bond_dims) == list(plain_host.bond_dims)}
 
     # ---------------------------------------------------------------- CPU baseline (oracle port)
     if not args.no_cpu_baseline:

@@ -115,7 +115,7 @@ int agb_contract_gate(int dtype, const void* A, const void* B, const void* U, vo
 int agb_two_site_plan(int dtype, int ngates, int64_t* desc_host, size_t* ws_bytes);
 #define AGB_RUN_REPAIR 1 /* flags: re-run, on the device, the vector phase of gates whose
                           * eigenvalue-guided eigenvector count fell short (AGB_D_NVEC = 0)
-                          * or whose eigenvectors overlap by more than 1e-2 after the
+                          * or whose eigenvectors overlap by more than 5e-2 after the
                           * eigensolver (then with the cluster tolerance widened to 1e-3);
                           * without it such gates report AGB_ERR_RANK / AGB_ERR_NOCONV */
 int agb_two_site_run(int dtype, int ngates, const int64_t* desc_dev, int64_t* desc_dev_out,

@@ -193,3 +193,47 @@ def test_rank_fallback_reruns_match_plain_run():
     ta = [t.cpu().numpy().astype(np.complex128) for t in plain.tensors]
     tb = [t.cpu().numpy().astype(np.complex128) for t in low.tensors]
     assert mps_fidelity(ta, tb) >= 1 - 1e-6
+
+
+def test_training_data_from_svd_events(tmp_path):
+    """The training pairs are read back from the SVD-event log: features and
+    kept rank / full size from records that carry them, others skipped."""
+    from atlasq_gb300 import svd_log
+    from atlasq_gb300.rank_predictor import training_data_from_events
+    lg = svd_log.SVDEventLogger(str(tmp_path))
+    lg.spectrum(bond=1, pre_rank=4, chi_max=32, tol=1e-8, total_weight=1.0, sigma=[1.0], keep=6, step=0,
+                chi_left=4, chi_right=8, features=[0.2, 0.3, 0.5, 0.1, 1.0], full=8)
+    lg.spectrum(bond=2, pre_rank=4, chi_max=32, tol=1e-8, total_weight=1.0, sigma=[1.0], keep=3, step=1,
+                chi_left=4, chi_right=8)
+    lg.spectrum(bond=3, pre_rank=8, chi_max=32, tol=1e-8, total_weight=1.0, sigma=[1.0], keep=16, step=2,
+                chi_left=8, chi_right=8, features=[0.3, 0.3, 0.9, 0.2, 0.5], full=16)
+    lg.close()
+    X, T = training_data_from_events(svd_log.read_events(str(tmp_path)))
+    assert X.shape == (2, 5) and X.dtype == np.float32
+    np.testing.assert_allclose(T, [0.75, 1.0])
+    np.testing.assert_allclose(X[1], [0.3, 0.3, 0.9, 0.2, 0.5], rtol=1e-6)
+
+
+@pytest.mark.gpu
+def test_training_pipeline_logs_trains_and_saves(tmp_path):
+    """log_plain_runs -> training_data_from_events -> train -> save / load on
+    a small hardware-efficient ansatz: one event per two-site gate, and the
+    reloaded network predicts what the trained one does."""
+    from atlasq_gb300 import svd_log
+    from atlasq_gb300.circuits import hea_circuit
+    from atlasq_gb300.rank_predictor import (RankPredictor, load_predictor, log_plain_runs, save_predictor,
+                                             training_data_from_events)
+    n, layers = 12, 4
+    path = log_plain_runs(lambda sd: hea_circuit(n, layers, seed=sd), [1, 2, 3], n, 32, 1e-8, str(tmp_path))
+    X, T = training_data_from_events(svd_log.read_events(path))
+    assert len(T) == 3 * layers * (n - 1)
+    assert np.all((T > 0) & (T <= 1))
+    rp = RankPredictor(seed=0)
+    hist = rp.train(X, T, steps=200)
+    assert hist[-1] < hist[0]
+    out = str(tmp_path / "w.npz")
+    save_predictor(rp, out, note="test")
+    rp2 = load_predictor(out)
+    a = rp.predict_fraction(X).cpu().numpy()
+    b = rp2.predict_fraction(X).cpu().numpy()
+    assert np.array_equal(a, b)
