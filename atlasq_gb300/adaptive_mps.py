@@ -149,10 +149,33 @@ class AdaptiveMPS:
         if self._res is not None:
             resident.leave(self)
 
+    def promotion_reachable(self) -> bool:
+        """Whether the complex128 promotion (adaptive_mps.py:266-274) can fire.
+
+        In complex64 the rank rule's cumulative sum is float32 (each partial
+        rounded), so a kept sigma_{k-1} either changed that sum (sigma_{k-1}^2
+        >= 2^-25 sigma_0^2) or, when the cap cut first, heads a tail of at most
+        n = 2 chi_cap values whose sum the float32 sum still resolves (>= 2^-26
+        of the total, or eps^2 of it when 1 - eps^2 is representable):
+        sigma_0 / sigma_{k-1} <= sqrt(n 2^26) (1.9e5 at chi_cap 256), so a
+        threshold at or above that bound is out of reach.  The one exception is
+        a rounding tie: a tail too small to change the partial sums that still
+        moves the float32 total up by one ulp lets the cap cut at a value below
+        that bound; a resident gate of that kind is counted in ``unpromoted``.
+        complex128 never promotes."""
+        if self.dtype_policy.default == _C128:
+            return False
+        n = 2 * max(self.chi_max_per_bond + [1])
+        return self.dtype_policy.default != torch.complex64 or \
+            self.dtype_policy.promote_if_cond_gt < math.sqrt(n * 2.0 ** 26)
+
     def _maybe_enter_resident(self):
+        # resident mode has no host step between gates, so it is entered only
+        # where the host path's per-gate decisions cannot fire: no predictor,
+        # budget or logs, and no reachable precision promotion
         if (self.device_resident and self._res is None and self.rank_predictor is None
                 and self.budget_global_mb is None and self.feature_log is None and self.svd_logger is None
-                and self.spectrum_log is None):
+                and self.spectrum_log is None and not self.promotion_reachable()):
             self._drain()
             resident.enter(self)
 

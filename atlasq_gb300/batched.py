@@ -132,6 +132,10 @@ class CapturedCircuit:
                 raise ValueError("capture needs device_resident instances")
             m._flush()
             m._maybe_enter_resident()
+            if m._res is None:
+                raise ValueError("capture needs instances that can run device-resident: no rank predictor, "
+                                 "budget or SVD logs, and a promotion threshold the rank rule cannot reach "
+                                 "(AdaptiveMPS.promotion_reachable)")
         device = insts[0].device
         self.device = device
         self.rounds = _schedule(insts, circuits)

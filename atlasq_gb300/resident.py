@@ -17,12 +17,15 @@ What a caller can observe:
 * Kernel-side failures are reported at that point instead of at the gate.
 * A gate whose eigenvalue-guided eigenvector count falls short is re-run with
   every vector on the device (the two-site repair pass), as the host path's
-  fallback would.  Resident mode does not re-run ill-conditioned gates in complex128
-  (adaptive_mps.py:268-274 promotes when sigma_0 / sigma_{k-1} > 1e6); such gates
-  are counted in ``AdaptiveMPS.unpromoted`` with the driver tag
-  ``gb300_gram_heevd_unpromoted``.  In complex64 with eps_bond <= 1e-4 the kept
-  spectrum cannot reach that ratio (the float32 rule drops values below ~1e-7
-  of the total weight).
+  fallback would.
+* Precision promotion (adaptive_mps.py:268-274, sigma_0 / sigma_{k-1} above
+  the policy's threshold) needs a host decision per gate, so an instance
+  enters resident mode only when its threshold is out of the float32 rank
+  rule's reach (``AdaptiveMPS.promotion_reachable``: below sqrt(2 chi_cap
+  2^26), 1.9e5 at chi_cap 256; the default 1e6 is above it) and otherwise runs
+  host-synchronised, where promotion happens.  A gate that nevertheless reports
+  a ratio above the threshold (only a float32 rounding tie in the rank rule's
+  total allows it) is counted in ``AdaptiveMPS.unpromoted``.
 """
 import ctypes
 import math

@@ -207,3 +207,20 @@ def test_pauli_fixture_records_the_reference_deviation():
         n = len(ps)
         T = T.reshape([2] * (2 * n)).permute([2 * i for i in range(n)] + [2 * i + 1 for i in range(n)])
         assert np.allclose(T.reshape(2 ** n, 2 ** n).numpy(), op, atol=1e-12)
+
+
+def test_promotion_reachability_bound():
+    """Resident execution is allowed only where the float32 rank rule cannot
+    reach the promotion threshold: sigma_0 / sigma_{k-1} <= sqrt(2 chi_cap 2^26)."""
+    import types
+    import torch
+    from atlasq_gb300.adaptive_mps import AdaptiveMPS, DTypePolicy
+
+    def reach(dt, thr, caps):
+        o = types.SimpleNamespace(dtype_policy=DTypePolicy(default=dt, promote_if_cond_gt=thr), chi_max_per_bond=caps)
+        return AdaptiveMPS.promotion_reachable(o)
+    assert not reach(torch.complex64, 1e6, [256] * 39)      # the default policy at chi 256
+    assert not reach(torch.complex64, 1e6, [512] * 63)
+    assert reach(torch.complex64, 1e5, [256] * 39)
+    assert reach(torch.complex64, 3.0, [16] * 9)
+    assert not reach(torch.complex128, 3.0, [16] * 9)        # complex128 never promotes

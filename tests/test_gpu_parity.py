@@ -597,24 +597,29 @@ def test_orthogonality_guard_repairs_overlapping_vectors():
         assert err <= 2 * opt + 1e-5, (oc, err, opt)
 
 
-def test_precision_promotion_matches_oracle():
+@pytest.mark.parametrize("resident", [False, True])
+def test_precision_promotion_matches_oracle(resident):
     """adaptive_mps.py:266-274: a gate whose kept spectrum spans more than
     promote_if_cond_gt (sigma_0 / sigma_{k-1}) is factorised again in
     complex128 and its two site tensors become complex128.  With the threshold
     lowered to 3, 14 of the 27 gates of a 10-qubit brickwork promote (their
     sigma_0 / sigma_{k-1} run from 1 to ~20, none within 7% of 3); the promoted
     gates, the kept ranks, the site dtypes and the state match the oracle run
-    with the same policy."""
+    with the same policy.  Asked for device-resident execution, an instance
+    whose threshold the rank rule can reach runs host-synchronised instead."""
     n = 10
     ops_ = haar_brickwork(n, 6, seed=21)
     pol = aq.DTypePolicy(default=torch.complex64, promote_if_cond_gt=3.0)
-    m = aq.AdaptiveMPS(n, bond_dim=1, eps_bond=1e-6, chi_max_per_bond=16, device=DEV, dtype_policy=pol)
+    m = aq.AdaptiveMPS(n, bond_dim=1, eps_bond=1e-6, chi_max_per_bond=16, device=DEV, dtype_policy=pol,
+                       device_resident=resident)
+    assert m.promotion_reachable()
     o = mo.OracleMPS(n, bond_dim=1, eps_bond=1e-6, chi_max_per_bond=16, dtype=np.complex64,
                      promote_if_cond_gt=3.0)
     for _, q, U in ops_:
         m.apply_two_site_gate(q, U)
         o.apply_two_site_gate(q, U.numpy())
     m.flush()
+    assert m._res is None and m.unpromoted == 0
     logs = m.statistics.logs
     ours = [d == "gb300_gram_heevd_c128" for d in logs["svd_driver"]]
     ref = [d == "complex128" for d in o.logs["dtype"]]
