@@ -24,10 +24,11 @@ AGB_ERR_TOO_LARGE = 8
 AGB_C64 = 0
 AGB_C128 = 1
 AGB_RUN_REPAIR = 1
+AGB_RUN_NO_GUARD = 2
 
 # descriptor fields (enum agb_desc_field)
 D_A, D_B, D_U, D_CHIL, D_CHIM, D_CHIR, D_CAP, D_EPS = 0, 1, 2, 3, 4, 5, 6, 7
-D_ANEW, D_BNEW, D_ELL, D_SEED, D_WS, D_CTOL = 8, 9, 10, 11, 12, 13
+D_ANEW, D_BNEW, D_ELL, D_SEED, D_WS, D_CTOL, D_ORTH, D_ORTHW = 8, 9, 10, 11, 12, 13, 14, 15
 D_K, D_EPSLOC, D_ENTROPY, D_CONDS, D_STATUS, D_TOTAL, D_NEEDED, D_MODE = 16, 17, 18, 19, 20, 21, 22, 23
 D_DIMS, D_BOND, D_CAPL, D_CAPM, D_CAPR, D_ELLPLAN, D_NVEC, D_REPAIR = 24, 25, 26, 27, 28, 29, 30, 31
 D_NFIELDS = 32

@@ -642,7 +642,7 @@ def apply_gate_entries(entries):
                              dtype=str(r["dtype"]), ms_elapsed=elapsed, condS=r["condS"])
 
 
-def _run_pipeline(entries, dt, ells, all_vectors=False, cluster_tol=None, spectra=False):
+def _run_pipeline(entries, dt, ells, all_vectors=False, cluster_tol=None, spectra=False, guard=True):
     """One batched launch sequence: plan -> run -> read ranks -> finalize.
     By default the device computes eigenvectors only for the eigenvalues the
     rank rule can keep (AGB_D_NVEC = 0); ``all_vectors`` computes every one
@@ -650,6 +650,10 @@ def _run_pipeline(entries, dt, ells, all_vectors=False, cluster_tol=None, spectr
     overrides the eigensolver's relative cluster tolerance (AGB_D_CTOL; the
     library default is 1e-5).  ``spectra`` also reads back each gate's
     computed singular values (result key ``sigma``, descending).
+    ``guard=False`` only measures the eigenvector orthogonality guard (result
+    keys ``orth`` / ``orth_w``: the largest overlap before the polish, and the
+    same weighted by the smaller eigenvalue over the largest) instead of
+    repairing or rejecting on it.
     Descriptor rows are built and read with NumPy; the two small copies per
     batch (descriptors up, results down) are the only host synchronisation."""
     lib = _lib.load()
@@ -713,7 +717,8 @@ def _run_pipeline(entries, dt, ells, all_vectors=False, cluster_tol=None, spectr
     # every vector on the device; AGB_ERR_RANK then only means a predicted ell
     # below the rank, which the caller re-runs at full size
     check(lib.agb_two_site_run(code, G, ptr(desc_dev), ptr(desc_dev), maxL, maxM, maxR, maxell,
-                               ptr(ws), wsz.value, stream, _lib.AGB_RUN_REPAIR), "two_site_run")
+                               ptr(ws), wsz.value, stream,
+                               _lib.AGB_RUN_REPAIR | (0 if guard else _lib.AGB_RUN_NO_GUARD)), "two_site_run")
     sig = None
     if spectra:
         cnt = max(1, maxell)
@@ -726,8 +731,8 @@ def _run_pipeline(entries, dt, ells, all_vectors=False, cluster_tol=None, spectr
     maxk = 1
     sts = out[:, _lib.D_STATUS].tolist()
     ks = out[:, _lib.D_K].tolist()
-    reals = np.ascontiguousarray(out[:, [_lib.D_EPSLOC, _lib.D_ENTROPY, _lib.D_CONDS, _lib.D_TOTAL]]
-                                 ).view(np.float64).tolist()
+    reals = np.ascontiguousarray(out[:, [_lib.D_EPSLOC, _lib.D_ENTROPY, _lib.D_CONDS, _lib.D_TOTAL, _lib.D_ORTH,
+                                         _lib.D_ORTHW]]).view(np.float64).tolist()
     modes = out[:, _lib.D_MODE].tolist()
     ellv = out[:, _lib.D_ELL].tolist()
     repv = out[:, _lib.D_REPAIR].tolist()
@@ -737,7 +742,8 @@ def _run_pipeline(entries, dt, ells, all_vectors=False, cluster_tol=None, spectr
         k = ks[g]
         r = {"status": st, "k": k, "eps_local": reals[g][0], "entropy": reals[g][1], "condS": reals[g][2],
              "chiL": chiL, "chiM": chiM, "chiR": chiR, "driver": "gb300_gram_heevd", "dtype": dt,
-             "mode": modes[g], "ell": ellv[g], "repair": repv[g], "total": reals[g][3]}
+             "mode": modes[g], "ell": ellv[g], "repair": repv[g], "total": reals[g][3],
+             "orth": math.sqrt(max(reals[g][4], 0.0)), "orth_w": reals[g][5]}
         if sig is not None:
             row_s = sig[g]
             r["sigma"] = row_s[:int(np.count_nonzero(row_s))].copy()

@@ -16,7 +16,7 @@ struct GemmProb {
   double alpha_re, alpha_im, beta_re, beta_im;
 };
 
-// Optional tensor-core context: scratch for the packed split operands and a
+// Optional tensor-core context: the tensor-core path's scratch token and a
 // device status word.  With a context whose scratch is large enough,
 // complex64 problems of at least 64 x 64 x 32 run on tcgen05 (gemm_tc.cu);
 // everything else runs on the SIMT kernel.

@@ -2,10 +2,11 @@
 #pragma once
 #include "gemm.cuh"
 
-// Device scratch for the packed split operands of `count` problems bounded by
-// maxM x maxN x maxK.
+// Device scratch of the tensor-core path for `count` problems bounded by
+// maxM x maxN x maxK (the split operands live in shared memory only, so this
+// is a small constant the dispatcher checks for).
 size_t tc_gemm_scratch_bytes(int count, int maxM, int maxN, int maxK);
-// Pack + GEMM.  `status` (device int) receives AGB_ERR_TIMEOUT if a bounded
-// wait expired; it is not cleared here.
+// The GEMM (operand split fused into the kernel).  `status` (device int)
+// receives AGB_ERR_TIMEOUT if a bounded wait expired; it is not cleared here.
 int launch_gemm_tc(const GemmProb* probs, int count, int maxM, int maxN, int maxK, void* scratch,
                    size_t scratch_bytes, int* status, cudaStream_t s);

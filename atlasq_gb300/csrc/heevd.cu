@@ -8,10 +8,12 @@ template <typename R> struct rlim;
 template <> struct rlim<float> {
   static AGB_HD float eps() { return FLT_EPSILON; }
   static AGB_HD float pivmin() { return 1e-30f; }
+  static AGB_HD float huge() { return FLT_MAX; }
 };
 template <> struct rlim<double> {
   static AGB_HD double eps() { return DBL_EPSILON; }
   static AGB_HD double pivmin() { return 1e-290; }
+  static AGB_HD double huge() { return DBL_MAX; }
 };
 
 void heevd_assign_scratch(HeevdProb& p, char* base, int esz) { heevd_assign_scratch_dev(p, base, esz); }
@@ -440,6 +442,21 @@ AGB_DEV bool in_cluster(const R* lam, int ell, int t, R tol) {
   return left || right;
 }
 
+// Lowest shift a member of the cluster [t0, t1) may take: halfway to the first
+// eigenvalue below the cluster.  The shifts of equal eigenvalues are walked
+// apart by 10 eps |lambda| each (LAPACK stein); in float32 a run of 64
+// near-equal members walks ~8e-5 |lambda|, which crosses into the next group
+// of a flat spectrum (measured: 64-qubit HEA gates, chi 512, whose members then
+// converged onto the neighbouring group's eigenvectors, overlaps up to 0.65).
+// Clamped there, inverse iteration from the member's random start still lands
+// in the cluster's invariant subspace, and the Gram-Schmidt passes separate
+// the members.
+template <typename R>
+AGB_DEV R shift_floor(const R* lam, int ell, int t1) {
+  if (t1 >= ell) return -rlim<R>::huge();
+  return R(0.5) * (lam[t1 - 1] + lam[t1]);
+}
+
 // LU with partial pivoting of T - lam I into the interleaved factor arrays
 // (column t of each), as in invit_kernel.
 template <typename R>
@@ -705,10 +722,12 @@ __global__ void __launch_bounds__(256) cluster_invit_kernel(const HeevdProb* __r
     R* shs = f;  // [c] shifts (c <= ell <= 5n)
     if (tid == 0) {
       R pv = 0;
+      const R lo = shift_floor(lamg, ell, t1);
       for (int j = t0; j < t1; ++j) {
         R sh = lamg[j];
         const R pj = R(10) * rlim<R>::eps() * fmax(fabs(sh), rlim<R>::pivmin());
         if (j > t0 && sh > pv - pj) sh = pv - pj;
+        sh = fmax(sh, lo);
         shs[j - t0] = sh;
         pv = sh;
       }
@@ -795,7 +814,8 @@ __global__ void __launch_bounds__(256) cluster_invit_kernel(const HeevdProb* __r
                 for (int jj = 0; jj < bw; ++jj) {
                   R a = 0;
 #pragma unroll
-                  for (int i = 0; i < 32; ++i) a += yr[i] * ctile[i * 32 + jj];
+                  for (int i = 0; i < 32; ++i)
+                    if (i < tw) a += yr[i] * ctile[i * 32 + jj];  // rows >= tw were not written
                   Zs[(int64_t)r * bw + jj] -= a;
                 }
               }
@@ -814,6 +834,7 @@ __global__ void __launch_bounds__(256) cluster_invit_kernel(const HeevdProb* __r
     return;
   }
   R prev = 0;
+  const R lo = shift_floor(lamg, ell, t1);
   for (int j = t0; j < t1; ++j) {
     if (tid == 0) {
       R sh = lamg[j];
@@ -822,6 +843,7 @@ __global__ void __launch_bounds__(256) cluster_invit_kernel(const HeevdProb* __r
       // the shifts of a long run of small eigenvalues far below the cluster
       const R pj = R(10) * rlim<R>::eps() * fmax(fabs(sh), rlim<R>::pivmin());
       if (j > t0 && sh > prev - pj) sh = prev - pj;
+      sh = fmax(sh, lo);
       s_shift = sh;
       tri_lu(d, e, n, sh, piv, f, f + n, f + 2 * n, f + 3 * n, f + 4 * n, 1, 0);
     }
@@ -853,8 +875,14 @@ __global__ void polish_setup_kernel(HeevdProb* __restrict__ probs, GemmProb* gp,
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= count) return;
   const HeevdProb P = probs[i];
-  const bool fwd = (step == 0);
-  if (fwd && !P.skip_vectors) probs[i].orth_max2 = 0u;
+  const bool fwd = (step & 1) == 0;  // even steps V -> V2, odd steps V2 -> V
+  if (step == 0 && !P.skip_vectors) {
+    probs[i].orth_max2 = 0u;
+    probs[i].orth_w2 = 0u;
+  }
+  // steps 2 and 3 only for the problems whose first product showed an overlap
+  // above kOrthPolish (two steps take an overlap d to ~0.42 d^4)
+  const bool idle = P.skip_vectors || (step >= 2 && !orth_above(P.orth_max2, kOrthPolish));
   const void* Vs = fwd ? P.V : P.V2;
   void* Vd = fwd ? P.V2 : P.V;
   const int64_t lds = fwd ? P.ldv : P.ell;
@@ -865,7 +893,7 @@ __global__ void polish_setup_kernel(HeevdProb* __restrict__ probs, GemmProb* gp,
   g.M = P.nvec; g.N = P.nvec; g.K = P.n;
   g.opA = 2; g.opB = 0;
   g.alpha_re = 1; g.alpha_im = 0; g.beta_re = 0; g.beta_im = 0;
-  if (P.skip_vectors) g.M = 0;
+  if (idle) g.M = 0;
   gp[i] = g;
   GemmProb h;
   h.A = Vs; h.B = P.M; h.D = Vd; h.Csrc = Vs;
@@ -873,7 +901,7 @@ __global__ void polish_setup_kernel(HeevdProb* __restrict__ probs, GemmProb* gp,
   h.M = P.n; h.N = P.nvec; h.K = P.nvec;
   h.opA = 0; h.opB = 0;
   h.alpha_re = -0.5; h.alpha_im = 0; h.beta_re = 1.5; h.beta_im = 0;
-  if (P.skip_vectors) h.M = 0;
+  if (idle) h.M = 0;
   gp[count + i] = h;
 }
 
@@ -884,10 +912,11 @@ __global__ void polish_setup_kernel(HeevdProb* __restrict__ probs, GemmProb* gp,
 // may mix among themselves and with the others at no cost to X V_k V_k^H,
 // since X maps them to ~0.  The largest |M_ij|^2 over those pairs (i > j)
 // is folded into P.orth_max2 (float bits; atomicMax on non-negative floats
-// orders like the values); a non-finite entry stores +inf.  Two
-// Newton-Schulz steps only reach float32 orthonormality from overlaps below
-// ~1e-2, so a larger value re-runs the problem's vector phase (the two-site
-// repair pass).  Grid: (problems, row groups).
+// orders like the values); a non-finite entry stores +inf.  The same pairs
+// weighted by lambda_i / lambda_0 of the smaller eigenvalue go to P.orth_w2
+// (reported only).  Above kOrthPolish the polish takes two more steps, above
+// kOrthGuard the two-site repair pass re-runs the vector phase (heevd.cuh).
+// Grid: (problems, row groups).
 template <typename CX>
 __global__ void __launch_bounds__(256) orth_guard_kernel(HeevdProb* __restrict__ probs) {
   typedef typename cx_traits<CX>::R R;
@@ -901,16 +930,24 @@ __global__ void __launch_bounds__(256) orth_guard_kernel(HeevdProb* __restrict__
   int kl = 0;
   while (kl < nv && lam[kl] > floor_) ++kl;  // descending: the checked columns are [0, kl)
   const CX* M = (const CX*)P.M;
-  float worst = 0.f;
-  for (int i = 1 + blockIdx.y; i < kl; i += gridDim.y)
+  float worst = 0.f, wworst = 0.f;
+  for (int i = 1 + blockIdx.y; i < kl; i += gridDim.y) {
+    const float wi = (float)(lam[i] / l0);  // the smaller eigenvalue of the pair, relative
     for (int j = threadIdx.x; j < i; j += blockDim.x) {
       const CX z = M[(int64_t)i * ell + j];
       const float a2 = (float)cabs2(z);
-      worst = (isfinite(z.x) && isfinite(z.y)) ? fmaxf(worst, a2) : __int_as_float(0x7f800000);
+      const bool fin = isfinite(z.x) && isfinite(z.y);
+      worst = fin ? fmaxf(worst, a2) : __int_as_float(0x7f800000);
+      wworst = fin ? fmaxf(wworst, a2 * wi) : __int_as_float(0x7f800000);
     }
+  }
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) worst = fmaxf(worst, __shfl_xor_sync(0xffffffffu, worst, o));
+  for (int o = 16; o > 0; o >>= 1) {
+    worst = fmaxf(worst, __shfl_xor_sync(0xffffffffu, worst, o));
+    wworst = fmaxf(wworst, __shfl_xor_sync(0xffffffffu, wworst, o));
+  }
   if ((threadIdx.x & 31) == 0 && worst > 0.f) atomicMax(&P.orth_max2, __float_as_uint(worst));
+  if ((threadIdx.x & 31) == 0 && wworst > 0.f) atomicMax(&P.orth_w2, __float_as_uint(wworst));
 }
 
 // V = Q Y, reflectors applied in pairs (j, j-1), each pair staged once per CTA
@@ -1115,17 +1152,22 @@ int launch_heevd_vectors(HeevdProb* probs, GemmProb* gp, int count, int maxn, in
   prof_mark(AGB_ST_POLISH, s);
   // Newton-Schulz V <- V (3I - V^H V) / 2: quadratic convergence.  The vectors
   // arrive within ~eps*||T||/gap of orthonormal (gaps below the cluster
-  // tolerance are handled by the cluster kernel), i.e. below ~1e-2 in float32,
-  // so two steps reach the float32 floor (an even count leaves the result in V).
-  for (int step = 0; step < 2; ++step) {
-    polish_setup_kernel<<<(count + 127) / 128, 128, 0, s>>>(probs, gp, count, step & 1);
+  // tolerance are handled by the cluster kernel), normally below 1e-2 in
+  // float32, so two steps reach the float32 floor; problems whose first
+  // product shows more take two more (an even count leaves the result in V).
+  // The extra steps run on the SIMT GEMM: they are rare, and a launch whose
+  // problems are all idle then costs one short wave of small CTAs instead of
+  // several waves of tensor-core CTAs that reserve ~200 KB of shared memory each.
+  for (int step = 0; step < 4; ++step) {
+    const GemmCtx* c = step < 2 ? ctx : nullptr;
+    polish_setup_kernel<<<(count + 127) / 128, 128, 0, s>>>(probs, gp, count, step);
     AGB_CHECK_LAUNCH();
-    if ((rc = launch_gemm_probs<CX>(gp, count, maxell, maxell, s, ctx, maxn))) return rc;
+    if ((rc = launch_gemm_probs<CX>(gp, count, maxell, maxell, s, c, maxn))) return rc;
     if (step == 0) {
       orth_guard_kernel<CX><<<dim3(count, 8), 256, 0, s>>>(probs);
       AGB_CHECK_LAUNCH();
     }
-    if ((rc = launch_gemm_probs<CX>(gp + count, count, maxn, maxell, s, ctx, maxell))) return rc;
+    if ((rc = launch_gemm_probs<CX>(gp + count, count, maxn, maxell, s, c, maxell))) return rc;
   }
   return AGB_OK;
 }
@@ -1163,6 +1205,7 @@ __global__ void heevd_setup_kernel(HeevdProb* probs, void* H, void* evecs, char*
   p.nvec = ell;
   p.redo = 0;
   p.orth_max2 = 0u;
+  p.orth_w2 = 0u;
   p.ctol = kClusterTol;
   p.fail = 0;
   heevd_assign_scratch_dev(p, scratch + (size_t)b * scratch_stride, esz);

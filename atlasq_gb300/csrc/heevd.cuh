@@ -19,29 +19,38 @@
 // Eigenvalues closer than kClusterTol * max|lambda| are solved as a cluster
 // (re-orthogonalised inverse iteration, LAPACK stein's scheme); wider gaps
 // leave inverse-iteration vectors within ~(bisection error / gap)^3 of
-// orthogonal, far below what the Newton-Schulz polish removes.  A problem whose
-// first polish product V^H V still shows an overlap above kOrthGuard has its
-// vector phase re-run with the wider kClusterTolWide (the repair pass of the
-// two-site pipeline).  The guard separates two measured populations: two
-// inverse-iteration vectors converged onto one eigenvector (the zero-pivot
-// Sturm defect) overlap by 0.48-0.56 and leave a direction missing, while
-// imprecise vectors of a near-degenerate group (64-qubit HEA gates, chi 512)
-// overlap by up to 0.022 and span the right subspace.  Two Newton-Schulz steps
-// take an overlap d to ~0.42 d^4 (3e-6 from 0.05), so everything below the
-// guard is polished to float32 orthonormality.  On dense spectra of large Gram
-// matrices (n >= 512) the wide tolerance chains hundreds of eigenvalues into
-// one cluster, so it is only a repair setting.
+// orthogonal, which the Newton-Schulz polish removes.  The first polish
+// product V^H V is checked over the eigenvectors above the Gram's float32
+// floor (the orthogonality guard):
+//  * an overlap above kOrthPolish gets two more polish steps (two steps take
+//    an overlap d to ~0.42 d^4, so four reach float32 orthonormality from
+//    below kOrthGuard).  Measured: on flat spectra (64-qubit HEA, chi 512, a
+//    near-degenerate group of 128 eigenvalues followed by neighbours 3e-3
+//    apart) the first product shows overlaps up to 0.09 while the polished
+//    factors reproduce X to the optimal truncation error;
+//  * an overlap above kOrthGuard marks vectors that converged onto the same
+//    eigenvector (measured: 0.48-0.56 when a zero pivot of the Sturm count was
+//    mis-ordered): the polish cannot restore the missing direction, so the
+//    problem's vector phase is re-run with the wider kClusterTolWide (the
+//    repair pass of the two-site pipeline).  On the 64-qubit HEA (chi 512,
+//    degenerate groups split by float32 rounding into neighbouring clusters)
+//    18% of gates exceed it in the first pass; re-run at 1e-3, 14 of 3 024
+//    still did, at 1e-2 two.
+// On dense spectra of large Gram matrices (n >= 512) a wide tolerance chains
+// hundreds of eigenvalues into one cluster, so it is only a repair setting.
 constexpr double kClusterTol = 1e-5;
-constexpr double kClusterTolWide = 1e-3;
-constexpr float kOrthGuard = 5e-2f;
-AGB_HD bool orth_exceeds(unsigned max2_bits) {
+constexpr double kClusterTolWide = 1e-2;
+constexpr float kOrthPolish = 1e-2f;
+constexpr float kOrthGuard = 0.3f;
+AGB_HD bool orth_above(unsigned max2_bits, float limit) {
   union {
     unsigned u;
     float f;
   } c;
   c.u = max2_bits;
-  return !(c.f <= kOrthGuard * kOrthGuard);  // NaN / inf included
+  return !(c.f <= limit * limit);  // NaN / inf included
 }
+AGB_HD bool orth_exceeds(unsigned max2_bits) { return orth_above(max2_bits, kOrthGuard); }
 
 struct HeevdProb {
   void* H;       // CX[n x ldh], Hermitian input, overwritten by the reduction
@@ -64,6 +73,7 @@ struct HeevdProb {
                      // may be lowered between the two phases; strides stay ell
   int redo;          // set by the two-site repair pass: this problem's vector phase runs again
   unsigned orth_max2;  // orthogonality guard: largest |(V^H V)_ij|^2 over the checked pairs (float bits)
+  unsigned orth_w2;    // largest |(V^H V)_ij|^2 * lambda_i / lambda_0 (i > j) over the same pairs (float bits)
   double ctol;       // cluster tolerance relative to max|lambda| (kClusterTol unless repaired)
   void* band;        // scratch of the two-stage tridiagonalisation (block-reflector factors,
                      // exchange rows, band-stage reflectors), tridiag_2stage.cu

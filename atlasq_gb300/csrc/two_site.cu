@@ -69,10 +69,10 @@ AGB_HD size_t header_bytes(int ng) {
 }
 AGB_HD int* status_word(char* ws, int ng) { return (int*)(ws + header_bytes(ng) - 256); }
 
-// Packed-operand scratch for the tensor-core GEMMs of a batch (complex64 only),
-// sized for the largest of Gram (n x n, K = m), X V (m x ell, K = n) and the
-// polish products (ell x ell, K = n; n x ell, K = ell); it occupies the last
-// bytes of the workspace.
+// Scratch of the tensor-core GEMMs of a batch (complex64 only), the largest
+// over Gram (n x n, K = m), X V (m x ell, K = n) and the polish products
+// (ell x ell, K = n; n x ell, K = ell); it occupies the last bytes of the
+// workspace (a token: the split operands live in shared memory).
 size_t tc_tail_bytes(int dtype, int ng, int maxm, int maxn, int maxell) {
   if (dtype != AGB_C64 || ng <= 0) return 0;
   size_t b = tc_gemm_scratch_bytes(ng, maxn, maxn, maxm);
@@ -132,6 +132,7 @@ __global__ void setup_kernel(int64_t* __restrict__ desc, int ng, char* ws, int e
   p.nvec = ell;
   p.redo = 0;
   p.orth_max2 = 0u;
+  p.orth_w2 = 0u;
   p.fail = 0;
   p.ctol = D[AGB_D_CTOL] ? dbits(D[AGB_D_CTOL]) : kClusterTol;
   heevd_assign_scratch_dev(p, slab + L.heevd, esz);
@@ -431,8 +432,10 @@ __global__ void __launch_bounds__(512) prerank_kernel(int64_t* __restrict__ desc
 template <typename CX>
 // pass: 0 first pass (a repair pass follows), 1 repair pass (only repaired
 // gates), 2 first pass with no repair pass.  In passes 1 and 2 a gate whose
-// eigenvectors failed the orthogonality guard reports AGB_ERR_NOCONV.
-__global__ void __launch_bounds__(1024) rank_kernel(int64_t* __restrict__ desc, int ng, char* ws, int pass) {
+// eigenvectors failed the orthogonality guard reports AGB_ERR_NOCONV unless
+// `guard` is 0 (the guard is then only reported).
+__global__ void __launch_bounds__(1024) rank_kernel(int64_t* __restrict__ desc, int ng, char* ws, int pass,
+                                                    int guard) {
   typedef typename cx_traits<CX>::R R;
   const bool f32 = sizeof(R) == 4;
   const int g = blockIdx.x;
@@ -533,7 +536,7 @@ __global__ void __launch_bounds__(1024) rank_kernel(int64_t* __restrict__ desc, 
     status = AGB_ERR_NOCONV;
     k = 0;
   }
-  if (pass != 0 && orth_exceeds(hp[g].orth_max2) && mode0 != 1) {  // eigenvectors not orthonormal, no repair left
+  if (guard && pass != 0 && orth_exceeds(hp[g].orth_max2) && mode0 != 1) {  // not orthonormal, no repair left
     status = AGB_ERR_NOCONV;
     k = 0;
   }
@@ -556,6 +559,8 @@ __global__ void __launch_bounds__(1024) rank_kernel(int64_t* __restrict__ desc, 
   D[AGB_D_STATUS] = status;
   D[AGB_D_TOTAL] = bitsd(total_d);
   D[AGB_D_NEEDED] = needed;
+  D[AGB_D_ORTH] = bitsd(mode0 == 1 ? 0.0 : (double)__uint_as_float(hp[g].orth_max2));
+  D[AGB_D_ORTHW] = bitsd(mode0 == 1 ? 0.0 : (double)__uint_as_float(hp[g].orth_w2));
 }
 
 // ------------------------------------------------------------------ scatter
@@ -633,7 +638,7 @@ __global__ void spectra_kernel(const int64_t* __restrict__ desc, const char* ws,
 // nvec < ell), or whose eigenvectors failed the orthogonality guard (then with
 // the wide cluster tolerance), runs its vector phase, X*V and rank selection
 // again with every vector; every other gate is skipped by those launches.
-__global__ void repair_setup_kernel(int64_t* __restrict__ desc, int ng, char* ws) {
+__global__ void repair_setup_kernel(int64_t* __restrict__ desc, int ng, char* ws, int guard) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= ng) return;
   int64_t* D = desc + (int64_t)g * AGB_D_NFIELDS;
@@ -642,7 +647,8 @@ __global__ void repair_setup_kernel(int64_t* __restrict__ desc, int ng, char* ws
   const int ell = (int)D[AGB_D_ELL];
   const int st = (int)D[AGB_D_STATUS];
   const bool short_count = st == AGB_ERR_RANK && hp[g].nvec < ell && D[AGB_D_MODE] == 0;
-  const bool overlap = orth_exceeds(hp[g].orth_max2) && D[AGB_D_MODE] == 0 && (st == AGB_OK || st == AGB_ERR_RANK);
+  const bool overlap =
+      guard && orth_exceeds(hp[g].orth_max2) && D[AGB_D_MODE] == 0 && (st == AGB_OK || st == AGB_ERR_RANK);
   if (short_count || overlap) {
     hp[g].redo = 1;
     hp[g].nvec = ell;
@@ -693,15 +699,16 @@ int run_impl(int ng, int64_t* desc, int maxL, int maxM, int maxR, int maxell, ch
   rc = launch_gemm_probs<CX>(gp + 3 * ng, ng, maxm, maxell, s, &ctx, maxn);
   if (rc) return rc;
   prof_mark(AGB_ST_RANK, s);
+  const int guard = (flags & AGB_RUN_NO_GUARD) ? 0 : 1;
   rank_kernel<CX><<<ng, 1024, 4 * (size_t)maxell * sizeof(double), s>>>(desc, ng, ws,
-                                                                          (flags & AGB_RUN_REPAIR) ? 0 : 2);
+                                                                          (flags & AGB_RUN_REPAIR) ? 0 : 2, guard);
   AGB_CHECK_LAUNCH();
   if (!(flags & AGB_RUN_REPAIR)) {
     prof_mark(AGB_ST_GAP, s);
     return AGB_OK;
   }
   // repair pass for gates whose guided eigenvector count was too small
-  repair_setup_kernel<<<(ng + 127) / 128, 128, 0, s>>>(desc, ng, ws);
+  repair_setup_kernel<<<(ng + 127) / 128, 128, 0, s>>>(desc, ng, ws, guard);
   AGB_CHECK_LAUNCH();
   rc = launch_heevd_vectors<CX>(hp, gp, ng, maxn, maxell, s, &ctx);
   if (rc) return rc;
@@ -709,7 +716,7 @@ int run_impl(int ng, int64_t* desc, int maxL, int maxM, int maxR, int maxell, ch
   rc = launch_gemm_probs<CX>(gp + 3 * ng, ng, maxm, maxell, s, &ctx, maxn);
   if (rc) return rc;
   prof_mark(AGB_ST_RANK, s);
-  rank_kernel<CX><<<ng, 1024, 4 * (size_t)maxell * sizeof(double), s>>>(desc, ng, ws, 1);
+  rank_kernel<CX><<<ng, 1024, 4 * (size_t)maxell * sizeof(double), s>>>(desc, ng, ws, 1, guard);
   AGB_CHECK_LAUNCH();
   prof_mark(AGB_ST_GAP, s);
   return AGB_OK;

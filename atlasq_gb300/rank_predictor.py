@@ -185,10 +185,12 @@ def collect_training_data(circuit_fn, seeds, n, chi, eps, device="cuda"):
 
 def log_plain_runs(circuit_fn, seeds, n, chi, eps, log_dir, device="cuda"):
     """Run the plain simulator (no predictor) on ``circuit_fn(seed)`` for every
-    seed with the SVD-event log on; returns the log file's path."""
+    seed with the SVD-event log on; returns the log file's path.  The number of
+    gates per SVD driver tag over all runs is left in ``log_plain_runs.drivers``."""
     from . import svd_log
     from .adaptive_mps import AdaptiveMPS
     logger = svd_log.SVDEventLogger(log_dir)
+    log_plain_runs.drivers = {}
     try:
         for sd in seeds:
             m = AdaptiveMPS(n, bond_dim=1, eps_bond=eps, chi_max_per_bond=chi, device=device)
@@ -200,6 +202,8 @@ def log_plain_runs(circuit_fn, seeds, n, chi, eps, log_dir, device="cuda"):
                 else:
                     m.apply_single_qubit_gate(q, U)
             m.flush()
+            for d in m.statistics.logs["svd_driver"]:
+                log_plain_runs.drivers[d] = log_plain_runs.drivers.get(d, 0) + 1
     finally:
         logger.close()
     return str(logger.path)
@@ -288,7 +292,8 @@ def _main(argv=None):
     save_predictor(pred, a.out, circuit=a.circuit, runs=a.runs, first_seed=a.first_seed, qubits=a.qubits,
                    layers=a.layers,
                    chi=a.chi, eps=a.eps, samples=int(len(T)))
-    print(json.dumps({"samples": int(len(T)), "log": path, "log_seconds": t_log, "train_seconds": t_train,
+    print(json.dumps({"samples": int(len(T)), "drivers": log_plain_runs.drivers, "log": path,
+                      "log_seconds": t_log, "train_seconds": t_train,
                       "final_loss": hist[-1], "val_mae_fraction": float(np.mean(np.abs(fv - T[val]))),
                       "val_under_predicted": float(np.mean(fv * (1 + pred.margin) < T[val])),
                       "out": a.out}), flush=True)

@@ -59,6 +59,10 @@ enum agb_desc_field {
   AGB_D_WS = 12,      /* (plan) byte offset of this gate's workspace slab      */
   AGB_D_CTOL = 13,    /* (in)  eigenvalue cluster tolerance relative to the largest
                        *       eigenvalue (double bits); 0 = the default 1e-5     */
+  AGB_D_ORTH = 14,    /* (out) largest |(V^H V)_ij|^2, i != j, before the polish, over
+                       *       eigenvectors above the Gram's float floor (double bits) */
+  AGB_D_ORTHW = 15,   /* (out) the same pairs weighted by lambda_i / lambda_0 of the
+                       *       smaller eigenvalue (double bits)                    */
   AGB_D_K = 16,       /* (out) kept rank                                       */
   AGB_D_EPSLOC = 17,  /* (out) eps_local (double bits)                         */
   AGB_D_ENTROPY = 18, /* (out) entropy in nats (double bits)                   */
@@ -84,7 +88,7 @@ enum agb_desc_field {
                        *       keep (from the eigenvalues, plus a pad); -1: all ell */
   AGB_D_REPAIR = 31,  /* (out) vector phase re-run on the device: bit 0 the guided
                        *       count fell short, bit 1 the eigenvectors failed the
-                       *       orthogonality guard (re-run with tolerance 1e-3)   */
+                       *       orthogonality guard (re-run with tolerance 1e-2)   */
   AGB_D_NFIELDS = 32
 };
 
@@ -115,9 +119,11 @@ int agb_contract_gate(int dtype, const void* A, const void* B, const void* U, vo
 int agb_two_site_plan(int dtype, int ngates, int64_t* desc_host, size_t* ws_bytes);
 #define AGB_RUN_REPAIR 1 /* flags: re-run, on the device, the vector phase of gates whose
                           * eigenvalue-guided eigenvector count fell short (AGB_D_NVEC = 0)
-                          * or whose eigenvectors overlap by more than 5e-2 after the
-                          * eigensolver (then with the cluster tolerance widened to 1e-3);
+                          * or whose eigenvectors overlap by more than 0.3 after the
+                          * eigensolver (then with the cluster tolerance widened to 1e-2);
                           * without it such gates report AGB_ERR_RANK / AGB_ERR_NOCONV */
+#define AGB_RUN_NO_GUARD 2 /* flags: measure the orthogonality guard (AGB_D_ORTH/ORTHW) but
+                            * neither repair nor reject on it */
 int agb_two_site_run(int dtype, int ngates, const int64_t* desc_dev, int64_t* desc_dev_out,
                      int max_chiL, int max_chiM, int max_chiR, int max_ell, void* ws, size_t ws_bytes,
                      void* stream, int flags);
@@ -268,7 +274,9 @@ int agb_mlp_adam(float* params, const float* grads, float* m, float* v, int step
                  float beta2, float eps, float weight_decay, void* stream);
 
 /* Batched complex64 GEMM on the tcgen05 tensor cores (3xTF32 split precision,
- * TMA-fed), strided batch: C[b] = alpha op(A[b]) op(B[b]) + beta C[b].
+ * the split into TF32 planes done in shared memory inside the kernel), strided
+ * batch: C[b] = alpha op(A[b]) op(B[b]) + beta C[b]; op is 'N', 'T', 'C' or 'R'
+ * (conjugated, not transposed).
  * Replaces the torch/cuBLAS complex matmuls of the reference path
  * (mps_complex.py:359-366, mps_pytorch.py:300-352, mpo_ops.py:1145).
  * ws: agb_cgemm_tc_workspace(batch, M, N, K) bytes.  If status_host is not
