@@ -42,7 +42,7 @@ constexpr int CONV_WARPS = 8;
 constexpr int NCONV = 32 * CONV_WARPS;                 // converter / epilogue threads (warps 0-7)
 constexpr int NTHREADS = NCONV + 32;                   // + warp 8: tensor memory and MMA issue
 constexpr int MMA_WARP = CONV_WARPS;
-constexpr int PER_A = BM * BK / NCONV, PER_B = BN * BK / NCONV;  // values per converter thread per k slice
+constexpr int QA = BM * BK / 4 / NCONV, QB = BN * BK / 4 / NCONV;  // quads (4 consecutive k) per thread per k slice
 constexpr unsigned WAIT_LIMIT = 1u << 26;              // bounded spin (~seconds)
 
 AGB_DEV uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -104,11 +104,11 @@ AGB_DEV void tmem_ld16(uint32_t taddr, float* v) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// x rounded to TF32 (10 explicit mantissa bits), round to nearest even.
 AGB_DEV float tf32_hi(float x) {
-  uint32_t b = __float_as_uint(x);
-  if ((b & 0x7F800000u) == 0x7F800000u) return x;  // inf / nan unchanged
-  b = (b + 0xFFFu + ((b >> 13) & 1u)) & 0xFFFFE000u;  // round to nearest even at 13 dropped bits
-  return __uint_as_float(b);
+  uint32_t b;
+  asm("cvt.rn.tf32.f32 %0, %1;" : "=r"(b) : "f"(x));
+  return __uint_as_float(b & 0xFFFFE000u);
 }
 
 // Byte offset of element (row r, k) in a plane tile of 128-byte rows (32 fp32)
@@ -116,25 +116,30 @@ AGB_DEV float tf32_hi(float x) {
 // (the tile starts on a 1024-byte boundary).
 AGB_DEV uint32_t sw128(int r, int k) { return (uint32_t)(r * 128 + (((k >> 2) ^ (r & 7)) << 4) + ((k & 3) << 2)); }
 
-AGB_DEV void st_shared_f32(uint32_t addr, float v) {
-  asm volatile("st.shared.f32 [%0], %1;" ::"r"(addr), "f"(v) : "memory");
+AGB_DEV void st_shared_v4(uint32_t addr, float a, float b, float c, float d) {
+  asm volatile("st.shared.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "f"(a), "f"(b), "f"(c), "f"(d) : "memory");
 }
 
-// Coordinates (row, k) inside the slice of the j-th value a converter thread
-// handles.  k contiguous in memory: a warp takes 32 consecutive k of one row.
-// Otherwise a warp takes an 8-row x 4-k block (lanes: row = lane % 8, k =
-// lane / 8; four 64-byte row segments per load), blocks b = w + 8 j with
-// k block b % 8 and row block b / 8.  Both mappings put a warp's 32 stores on
-// 32 different banks of the swizzled tile (chunk (k/4) ^ (row % 8), word k % 4).
-AGB_DEV void slice_coord(bool k_contig, int ct, int j, int& r, int& k) {
+// A converter thread handles quads: 4 consecutive k of one row, which are
+// one 16-byte chunk of the swizzled tile (one vector store per plane).  The
+// j-th quad of thread ct:
+//  * k contiguous in memory: a warp takes 4 rows x 32 k (lanes: row
+//    lane / 8, quad lane % 8), rows 4 (w + 8 j) ..; each row is one 256-byte
+//    read;
+//  * otherwise: a warp takes 32 consecutive rows x one quad (lanes: row),
+//    blocks b = w + 8 j with quad b % 8 and 32-row chunk b / 8; each k of the
+//    quad is one 256-byte read.
+// Either way each 8-lane phase of a vector store covers the 8 chunk positions
+// of the 128-byte swizzle (chunk (k/4) ^ (row % 8)): no bank conflicts.
+AGB_DEV void quad_coord(bool k_contig, int ct, int j, int& r, int& k4) {
   const int lane = ct & 31, w = ct >> 5;
   if (k_contig) {
-    r = w + CONV_WARPS * j;
-    k = lane;
+    r = 4 * (w + CONV_WARPS * j) + (lane >> 3);
+    k4 = 4 * (lane & 7);
   } else {
     const int b = w + CONV_WARPS * j;
-    k = 4 * (b & 7) + (lane >> 3);
-    r = 8 * (b >> 3) + (lane & 7);
+    k4 = 4 * (b & 7);
+    r = 32 * (b >> 3) + lane;
   }
 }
 
@@ -160,32 +165,42 @@ AGB_DEV Operand operand(const GemmProb& P, int which) {
   o.conj = (op == 2 || op == 3);
   return o;
 }
-template <int PER>
+template <int NQ>
 AGB_DEV void load_slice(const Operand& o, int r0, int k0, int ct, float2* v) {
 #pragma unroll
-  for (int j = 0; j < PER; ++j) {
-    int r, k;
-    slice_coord(o.k_contig, ct, j, r, k);
+  for (int j = 0; j < NQ; ++j) {
+    int r, k4;
+    quad_coord(o.k_contig, ct, j, r, k4);
     r += r0;
-    k += k0;
-    float2 x = make_float2(0.f, 0.f);
-    if (r < o.rows && k < o.K) x = o.k_contig ? o.p[(int64_t)r * o.ld + k] : o.p[(int64_t)k * o.ld + r];
-    v[j] = x;
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      const int k = k0 + k4 + t;
+      float2 x = make_float2(0.f, 0.f);
+      if (r < o.rows && k < o.K) x = o.k_contig ? o.p[(int64_t)r * o.ld + k] : o.p[(int64_t)k * o.ld + r];
+      v[4 * j + t] = x;
+    }
   }
 }
-template <int PER>
+template <int NQ>
 AGB_DEV void store_slice(const Operand& o, uint32_t tile, int plane_bytes, int ct, const float2* v) {
 #pragma unroll
-  for (int j = 0; j < PER; ++j) {
-    int r, k;
-    slice_coord(o.k_contig, ct, j, r, k);
-    const float re = v[j].x, im = o.conj ? -v[j].y : v[j].y;
-    const float rh = tf32_hi(re), ih = tf32_hi(im);
-    const uint32_t a = tile + sw128(r, k);
-    st_shared_f32(a, rh);
-    st_shared_f32(a + plane_bytes, re - rh);
-    st_shared_f32(a + 2 * plane_bytes, ih);
-    st_shared_f32(a + 3 * plane_bytes, im - ih);
+  for (int j = 0; j < NQ; ++j) {
+    int r, k4;
+    quad_coord(o.k_contig, ct, j, r, k4);
+    float rh[4], rl[4], ih[4], il[4];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      const float re = v[4 * j + t].x, im = o.conj ? -v[4 * j + t].y : v[4 * j + t].y;
+      rh[t] = tf32_hi(re);
+      ih[t] = tf32_hi(im);
+      rl[t] = re - rh[t];
+      il[t] = im - ih[t];
+    }
+    const uint32_t a = tile + sw128(r, k4);
+    st_shared_v4(a, rh[0], rh[1], rh[2], rh[3]);
+    st_shared_v4(a + plane_bytes, rl[0], rl[1], rl[2], rl[3]);
+    st_shared_v4(a + 2 * plane_bytes, ih[0], ih[1], ih[2], ih[3]);
+    st_shared_v4(a + 3 * plane_bytes, il[0], il[1], il[2], il[3]);
   }
 }
 
@@ -228,17 +243,17 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     const Operand oa = operand(P, 0), ob = operand(P, 1);
     for (int kt = 0; kt < nk; ++kt) {
       const int s = kt % STAGES;
-      float2 va[PER_A], vb[PER_B];
-      load_slice<PER_A>(oa, m0, kt * BK, ct, va);  // in flight while the stage drains
-      load_slice<PER_B>(ob, n0, kt * BK, ct, vb);
+      float2 va[4 * QA], vb[4 * QB];
+      load_slice<QA>(oa, m0, kt * BK, ct, va);  // in flight while the stage drains
+      load_slice<QB>(ob, n0, kt * BK, ct, vb);
       if (kt >= STAGES && !mbar_wait(&empty[s], ((kt / STAGES) - 1) & 1)) {
         *abort_flag = 1;
         break;
       }
       if (*abort_flag) break;
       const uint32_t st = smem_u32(smem + s * STAGE_BYTES);
-      store_slice<PER_A>(oa, st, TILE_A, ct, va);
-      store_slice<PER_B>(ob, st + 4 * TILE_A, TILE_B, ct, vb);
+      store_slice<QA>(oa, st, TILE_A, ct, va);
+      store_slice<QB>(ob, st + 4 * TILE_A, TILE_B, ct, vb);
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // visible to the tensor core
       mbar_arrive(&full[s]);
     }
