@@ -423,12 +423,13 @@ __global__ void __launch_bounds__(128) invit_kernel(const HeevdProb* __restrict_
 
 // ------------------------------------------------------------------ stage 4
 // Eigenvalue clusters (consecutive eigenvalues closer than tolrel * max|lambda|)
-// are solved member by member, as LAPACK's stein does: each member's iterate
-// is re-orthogonalised (classical Gram-Schmidt, twice) against the members
-// already computed before every inverse-iteration solve, and members' shifts
-// are separated by a few ulps.  This keeps the iterates from collapsing onto
-// one direction when T splits (exactly degenerate eigenvalues) or when the
-// cluster sits at the noise floor of the Gram matrix.  One CTA per cluster.
+// are solved with LAPACK stein's ingredients, its members in parallel: each
+// member shifted by its own eigenvalue (member_shift), one LU per member, and
+// two rounds of [one inverse-iteration solve
+// of every member from its own random start; Gram-Schmidt (classical, twice)
+// over the cluster in member order].  This keeps the iterates from collapsing
+// onto one direction when T splits (exactly degenerate eigenvalues) or when
+// the cluster sits at the noise floor of the Gram matrix.  One CTA per cluster.
 template <typename R>
 AGB_DEV R cluster_tol(const R* lam, int ell, double tolrel) {
   const R scale = fmax(fabs(lam[0]), fabs(lam[ell - 1]));
@@ -442,19 +443,25 @@ AGB_DEV bool in_cluster(const R* lam, int ell, int t, R tol) {
   return left || right;
 }
 
-// Lowest shift a member of the cluster [t0, t1) may take: halfway to the first
-// eigenvalue below the cluster.  The shifts of equal eigenvalues are walked
-// apart by 10 eps |lambda| each (LAPACK stein); in float32 a run of 64
-// near-equal members walks ~8e-5 |lambda|, which crosses into the next group
-// of a flat spectrum (measured: 64-qubit HEA gates, chi 512, whose members then
-// converged onto the neighbouring group's eigenvectors, overlaps up to 0.65).
-// Clamped there, inverse iteration from the member's random start still lands
-// in the cluster's invariant subspace, and the Gram-Schmidt passes separate
-// the members.
+// Shift of cluster member j: its own eigenvalue.  LAPACK's stein walks the
+// shifts of near-equal members apart by 10 eps |lambda| each, which is
+// harmless in double precision but in float32 moves the last members of a
+// cluster by ~1e-6 |lambda| per member, toward the first eigenvalue below
+// the cluster.  Measured on 64-qubit HEA gates (chi 512): eight members within
+// 6.6e-6 lambda_0 of each other and the next eigenvalue 1.2e-5 below; the
+// walked shift of the eighth member amplified that outside eigenvector about
+// a sixth as much as its own, and after the Gram-Schmidt pass had removed the
+// directions of the first seven members, what remained was 92% the outside
+// eigenvector.  With unwalked shifts the outside component is suppressed by
+// (bisection error / gap) per solve; members with equal shifts still get
+// independent iterates from their own random starts, which Gram-Schmidt
+// separates.  The shift is also kept above the midpoint to the eigenvalue
+// below the cluster.
 template <typename R>
-AGB_DEV R shift_floor(const R* lam, int ell, int t1) {
-  if (t1 >= ell) return -rlim<R>::huge();
-  return R(0.5) * (lam[t1 - 1] + lam[t1]);
+AGB_DEV R member_shift(const R* lam, int ell, int j, int t1) {
+  const R sh = lam[j];
+  if (t1 >= ell) return sh;
+  return fmax(sh, R(0.5) * (lam[t1 - 1] + lam[t1]));
 }
 
 // LU with partial pivoting of T - lam I into the interleaved factor arrays
@@ -715,22 +722,14 @@ __global__ void __launch_bounds__(256) cluster_invit_kernel(const HeevdProb* __r
   const int64_t L = ell;
   R* Y = (R*)P.Y;
   const int c = t1 - t0;
-  if (c >= 3) {
+  if (c >= 2) {
     // Members in parallel (LAPACK stein's iteration with the solves of all
-    // members at once): separated shifts; one LU per member (global, column j);
-    // two rounds of [solve every member; Gram-Schmidt in member order].
+    // members at once): each member's own eigenvalue as its shift; one LU per
+    // member (global, column j); two rounds of [solve every member;
+    // Gram-Schmidt in member order].
     R* shs = f;  // [c] shifts (c <= ell <= 5n)
     if (tid == 0) {
-      R pv = 0;
-      const R lo = shift_floor(lamg, ell, t1);
-      for (int j = t0; j < t1; ++j) {
-        R sh = lamg[j];
-        const R pj = R(10) * rlim<R>::eps() * fmax(fabs(sh), rlim<R>::pivmin());
-        if (j > t0 && sh > pv - pj) sh = pv - pj;
-        sh = fmax(sh, lo);
-        shs[j - t0] = sh;
-        pv = sh;
-      }
+      for (int j = t0; j < t1; ++j) shs[j - t0] = member_shift(lamg, ell, j, t1);
     }
     __syncthreads();
     R* lu = (R*)P.lu;
@@ -833,38 +832,6 @@ __global__ void __launch_bounds__(256) cluster_invit_kernel(const HeevdProb* __r
     }
     return;
   }
-  R prev = 0;
-  const R lo = shift_floor(lamg, ell, t1);
-  for (int j = t0; j < t1; ++j) {
-    if (tid == 0) {
-      R sh = lamg[j];
-      // separate the shifts (descending) by a perturbation relative to the
-      // eigenvalue, as LAPACK's stein does: an absolute one (eps * ||T||) walks
-      // the shifts of a long run of small eigenvalues far below the cluster
-      const R pj = R(10) * rlim<R>::eps() * fmax(fabs(sh), rlim<R>::pivmin());
-      if (j > t0 && sh > prev - pj) sh = prev - pj;
-      sh = fmax(sh, lo);
-      s_shift = sh;
-      tri_lu(d, e, n, sh, piv, f, f + n, f + 2 * n, f + 3 * n, f + 4 * n, 1, 0);
-    }
-    for (int r = tid; r < n; r += nt) ycol[r] = (R)philox_normal(P.seed, (uint64_t)j * (uint64_t)n + r, 0x11u);
-    __syncthreads();
-    prev = s_shift;
-    for (int it = 0; it < 2; ++it) {
-      cgs2_normalize(ycol, Y, n, L, t0, j, coef, red, part);
-      // (the prefetching solve with unit scale: the same operations as tri_solve)
-      if (tid == 0) s_nrm = tri_solve_pf(ycol, n, f, f + n, f + 2 * n, f + 3 * n, f + 4 * n, 1, 0, piv, R(1));
-      __syncthreads();
-      if (!(s_nrm < R(1e300)) || !(s_nrm > R(0))) {
-        for (int r = tid; r < n; r += nt)
-          ycol[r] = (R)philox_normal(P.seed ^ 0xABCDEFull, (uint64_t)(j + it + 1) * (uint64_t)n + r, 0x13u);
-        __syncthreads();
-      }
-    }
-    cgs2_normalize(ycol, Y, n, L, t0, j, coef, red, part);
-    for (int r = tid; r < n; r += nt) Y[(int64_t)r * L + j] = ycol[r];
-    __syncthreads();
-  }
 }
 
 // ------------------------------------------------------------------ stage 5 (backtransform2_kernel below)
@@ -950,6 +917,30 @@ __global__ void __launch_bounds__(256) orth_guard_kernel(HeevdProb* __restrict__
   if ((threadIdx.x & 31) == 0 && wworst > 0.f) atomicMax(&P.orth_w2, __float_as_uint(wworst));
 }
 
+// c_p = v_{j-1}^H v_j for the reflector pairs (j, j-1), j = n-2-2p, that the
+// back-transformation applies together (v_j[j+1] = 1, v_j[r] = H[j][r] for
+// r > j+1; v_{j-1}[j] = 1, v_{j-1}[r] = H[j-1][r] for r > j).  One warp per
+// pair; the result goes to P.lu, which the vector phase no longer needs.
+template <typename CX>
+__global__ void __launch_bounds__(256) bt_pair_coef_kernel(const HeevdProb* __restrict__ probs) {
+  const HeevdProb P = probs[blockIdx.y];
+  if (P.skip_vectors) return;
+  const int n = P.n, lane = threadIdx.x & 31;
+  const int pi = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int j = n - 2 - 2 * pi;
+  if (j < 1) return;
+  const CX* H = (const CX*)P.H;
+  const CX* row = H + (int64_t)j * P.ldh;
+  const CX* row2 = H + (int64_t)(j - 1) * P.ldh;
+  CX c = czero<CX>();
+  for (int r = j + 1 + lane; r < n; r += 32) {
+    const CX v1 = (r == j + 1) ? mk<CX>(1, 0) : row[r];
+    cfmac(c, row2[r], v1);
+  }
+  c = warp_csum(c);
+  if (lane == 0) ((CX*)P.lu)[pi] = c;
+}
+
 // V = Q Y, reflectors applied in pairs (j, j-1), each pair staged once per CTA
 // in shared memory (double-buffered, one barrier per pair); each warp owns two
 // columns of Y held in registers.  WARPS warps per CTA -> 2*WARPS columns.
@@ -979,6 +970,7 @@ __global__ void __launch_bounds__(WARPS * 32) backtransform2_kernel(const HeevdP
   }
   const CX* H = (const CX*)P.H;
   const CX* tau = (const CX*)P.tau;
+  const CX* pair_coef = (const CX*)P.lu;  // free after inverse iteration
   // the rows of the next pair are read from global memory one pair ahead
   // (registers), so the L2 round trip overlaps the current pair's work;
   // thread tid stages rows tid + WARPS * 32 * u
@@ -1014,7 +1006,9 @@ __global__ void __launch_bounds__(WARPS * 32) backtransform2_kernel(const HeevdP
     __syncthreads();
     const bool a1 = (t1.x != R(0) || t1.y != R(0)), a2 = (t2.x != R(0) || t2.y != R(0));
     if (!a1 && !a2) continue;
-    CX d10 = czero<CX>(), d11 = czero<CX>(), d20 = czero<CX>(), d21 = czero<CX>(), c = czero<CX>();
+    // v_{j-1}^H v_j, the same for every column: from bt_pair_coef_kernel
+    const CX c = (j >= 1) ? pair_coef[(n - 2 - j) >> 1] : czero<CX>();
+    CX d10 = czero<CX>(), d11 = czero<CX>(), d20 = czero<CX>(), d21 = czero<CX>();
     // v_j and v_{j-1} are zero in rows < j: chunks of 32 rows below that are
     // skipped (a warp-uniform test, so the register arrays keep static indices)
 #pragma unroll
@@ -1026,14 +1020,12 @@ __global__ void __launch_bounds__(WARPS * 32) backtransform2_kernel(const HeevdP
         cfmac(d11, v1, z1[k]);
         cfmac(d20, v2, z0[k]);
         cfmac(d21, v2, z1[k]);
-        cfmac(c, v2, v1);
       }
     }
     d10 = warp_csum(d10);
     d11 = warp_csum(d11);
     d20 = warp_csum(d20);
     d21 = warp_csum(d21);
-    c = warp_csum(c);
     const CX s10 = cmul(t1, d10), s11 = cmul(t1, d11);
     const CX s20 = cmul(t2, csub(d20, cmul(c, s10))), s21 = cmul(t2, csub(d21, cmul(c, s11)));
 #pragma unroll
@@ -1066,6 +1058,9 @@ int launch_bt(const HeevdProb* probs, int count, int maxell, cudaStream_t s) {
     agb_note_error(__FILE__, __LINE__, oe);
     return AGB_ERR_CUDA;
   }
+  const int npairs = NK * 32 / 2;  // pairs for the largest n this instance handles
+  bt_pair_coef_kernel<CX><<<dim3((npairs + 7) / 8, count), 256, 0, s>>>(probs);
+  AGB_CHECK_LAUNCH();
   dim3 grid((maxell + 2 * WARPS - 1) / (2 * WARPS), count);
   backtransform2_kernel<CX, NK, WARPS><<<grid, WARPS * 32, smem, s>>>(probs);
   AGB_CHECK_LAUNCH();

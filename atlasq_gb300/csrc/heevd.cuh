@@ -24,18 +24,17 @@
 // floor (the orthogonality guard):
 //  * an overlap above kOrthPolish gets two more polish steps (two steps take
 //    an overlap d to ~0.42 d^4, so four reach float32 orthonormality from
-//    below kOrthGuard).  Measured: on flat spectra (64-qubit HEA, chi 512, a
-//    near-degenerate group of 128 eigenvalues followed by neighbours 3e-3
-//    apart) the first product shows overlaps up to 0.09 while the polished
+//    below kOrthGuard).  Measured: on flat spectra (64-qubit HEA, chi 512)
+//    2% of gates show overlaps between 1e-2 and 0.29, and the polished
 //    factors reproduce X to the optimal truncation error;
 //  * an overlap above kOrthGuard marks vectors that converged onto the same
 //    eigenvector (measured: 0.48-0.56 when a zero pivot of the Sturm count was
 //    mis-ordered): the polish cannot restore the missing direction, so the
 //    problem's vector phase is re-run with the wider kClusterTolWide (the
-//    repair pass of the two-site pipeline).  On the 64-qubit HEA (chi 512,
-//    degenerate groups split by float32 rounding into neighbouring clusters)
-//    18% of gates exceed it in the first pass; re-run at 1e-3, 14 of 3 024
-//    still did, at 1e-2 two.
+//    repair pass of the two-site pipeline).  On the 64-qubit HEA (chi 512)
+//    18% of gates exceeded it while cluster shifts were walked apart
+//    (member_shift in heevd.cu has why); since, none of 3 024 in the first
+//    pass.
 // On dense spectra of large Gram matrices (n >= 512) a wide tolerance chains
 // hundreds of eigenvalues into one cluster, so it is only a repair setting.
 constexpr double kClusterTol = 1e-5;

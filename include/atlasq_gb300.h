@@ -190,13 +190,17 @@ int agb_qr(int dtype, const void* A, int M, int N, int transA, void* Q, void* R,
 /* Allocation-free variant of agb_qr (no counterpart in the reference).
  * For callers that cannot allocate device memory -- e.g. a host runtime that
  * reaches this library only through the C ABI with device pointers handed to
- * it by the owner of the GPU memory.  Same arguments and results as agb_qr but
- * no workspace: the scratch is a fixed device array of AGB_QR_NOALLOC_MAX_BYTES
- * (8 MiB, held by every GPU that loads the library) -- problems needing more
- * (agb_qr_workspace(dtype, M, N) > the limit) return AGB_ERR_TOO_LARGE.  The
- * first call on a device looks up the array's address (cudaGetSymbolAddress):
- * make it before any stream capture.  All calls share the array, so calls that
- * overlap on the GPU race; serialise them.  Allocates nothing. */
+ * it by the owner of the GPU memory.  Same arguments as agb_qr but no
+ * workspace: it always runs the single-CTA Householder kernel, whose scratch
+ * (the working copy of op(A), M*N elements; the reflector scalars,
+ * min(M,N); the Q block, M*min(M,N); each rounded up to 256 bytes) lives in a
+ * fixed device array of AGB_QR_NOALLOC_MAX_BYTES (8 MiB, held by every GPU
+ * that loads the library) -- larger problems return AGB_ERR_TOO_LARGE.  For
+ * M*N >= 4096, where agb_qr uses its blocked cluster kernels, the two agree
+ * to rounding, not bit for bit.  The first call on a device looks up the
+ * array's address (cudaGetSymbolAddress): make it before any stream capture.
+ * All calls share the array, so calls that overlap on the GPU race;
+ * serialise them.  Allocates nothing. */
 #define AGB_QR_NOALLOC_MAX_BYTES (8u << 20)
 int agb_qr_noalloc(int dtype, const void* A, int M, int N, int transA, void* Q, void* R, int trans_out,
                    void* stream);

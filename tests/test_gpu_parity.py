@@ -584,20 +584,23 @@ def test_near_degenerate_leading_group_n512():
 
 
 def test_orthogonality_guard_repairs_overlapping_vectors():
-    """With the cluster tolerance forced to ~0 (AGB_D_CTOL), a four-fold
-    degenerate leading group is solved member by member and inverse iteration
-    returns overlapping vectors inside the degenerate subspace.  The guard on
-    the first Newton-Schulz product V^H V flags it, the repair pass re-runs the
-    vector phase with the 1e-2 cluster tolerance, and the result is again the
-    optimal truncation."""
-    lead = np.full(4, 1.0)
+    """With the cluster tolerance forced to ~0 (AGB_D_CTOL), four leading
+    eigenvalues of X^H X spaced 2e-7 apart (below the float32 Gram's
+    resolution) are solved one by one by inverse iteration, which returns
+    vectors mixed inside their common subspace.  The guard on the first
+    Newton-Schulz product V^H V flags overlaps above 0.3, the repair pass
+    re-runs the vector phase with the 1e-2 cluster tolerance, and every result
+    is again the optimal truncation."""
+    lead = 1.0 - 2e-7 * np.arange(4)
     rest = 0.6 * np.exp(-np.arange(60) / 6.0)
     A, B = _planted(32, lead, rest, seed=5)
-    for oc in range(4):
+    repaired = 0
+    for oc in range(8):
         r, err, opt = _run_planted(A, B, 24, 1e-8, oc, True, cluster_tol=1e-30)
-        assert r["repair"] & 2, (oc, r["repair"])
-        assert r["status"] == 0
+        repaired += bool(r["repair"] & 2)
+        assert r["status"] == 0, (oc, r["status"])
         assert err <= 2 * opt + 1e-5, (oc, err, opt)
+    assert repaired >= 1, repaired
 
 
 @pytest.mark.parametrize("resident", [False, True])

@@ -54,7 +54,9 @@ def _qr(lib, fn, A, M, N, trans, dtype):
 @pytest.mark.parametrize("dtype", [torch.complex64, torch.complex128])
 def test_noalloc_qr_matches_regular_entry_point_twice(dtype):
     lib = _lib.load()
-    cases = [((96, 40), False, 1), ((33, 70), True, 2)]  # two calls in a row, different inputs
+    # two calls in a row with different inputs, then a size where agb_qr takes its
+    # blocked cluster kernels (M*N >= 4096) while noalloc stays single-CTA
+    cases = [((96, 40), False, 1), ((33, 70), True, 2), ((256, 128), False, 3)]
     for (rows, cols), trans, seed in cases:
         A = _rand((rows, cols), dtype, seed)
         M, N = (cols, rows) if trans else (rows, cols)
@@ -71,7 +73,6 @@ def test_noalloc_qr_matches_regular_entry_point_twice(dtype):
 def test_noalloc_rejects_problems_beyond_the_fixed_scratch():
     lib = _lib.load()
     M, N = 2048, 1024  # complex64 working copy alone is 16 MiB > 8 MiB
-    assert lib.agb_qr_workspace(_lib.AGB_C64, M, N) > (8 << 20)
     dummy = torch.empty(1, dtype=torch.complex64, device=DEV)
     rc = lib.agb_qr_noalloc(_lib.AGB_C64, _lib.ptr(dummy), M, N, 0, _lib.ptr(dummy), _lib.ptr(dummy), 0,
                             _lib.stream_ptr(DEV))
