@@ -19,6 +19,7 @@ Lines printed (rank 0, one JSON object):
            contraction + torch.linalg.svd (cuSOLVER), for the plain-form comparison
   learned  the host-synchronised pipeline with the learned rank predictor sizing
            each gate's eigensolver (weights shipped in atlasq_gb300/data/)
+  graph_replay  the same circuit captured once as a CUDA graph and replayed
   fidelity_vs_fp64  |<psi|psi_fp64>|^2 of each arm's final state against this
            package's complex128 run of the same circuit
 
@@ -413,6 +414,10 @@ def main():
     ap.add_argument("--workload", default="brickwork40", choices=["brickwork40", "batch256", "sample50", "hea64"],
                     help="brickwork40 is the headline; the others are the secondary workloads")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-rank arm")
+    ap.add_argument("--no-graph", action="store_true", help="skip the CUDA-graph replay line")
+    ap.add_argument("--two-stage", action="store_true",
+                    help="use the two-stage tridiagonalisation (band reduction + bulge chasing) instead of the "
+                         "one-stage cluster kernel, for comparison")
     args = ap.parse_args()
     if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
         # one process per GPU: relaunch this command under torch.distributed.run
@@ -436,6 +441,8 @@ def main():
     import atlasq_gb300 as aq
     from atlasq_gb300 import _lib
     lib = _lib.load()
+    if args.two_stage:
+        _lib.check(lib.agb_set_tridiag_stages(0), "set_tridiag_stages")
     device = torch.device("cuda", local)
     torch.cuda.set_device(device)
     ops_host = make_circuit()
@@ -588,9 +595,37 @@ def main():
             "config": {"workload": WORKLOAD, "gates_per_step": ngates, "parallelism": f"replicas x{ws}",
                        "l2": "flushed between timed steps (2x L2 write)",
                        "precision": "complex64; Gram / X.V / polish GEMMs on tcgen05 (3xTF32), FP32 eigensolver",
+                       "tridiagonalisation": ("two-stage (band reduction + bulge chasing)" if args.two_stage else
+                                              "one-stage, matrix in cluster shared memory"),
                        "execution": "device-resident (no host sync between batches)" if RESIDENT else
                                     "host-synchronised (ranks read back after every batch)"},
             "clocks": clocks, "gpu_launches": launches, "e2e": e2e, "roofline": roof, "other_mode": other_mode}
+
+    # ---------------------------------------------------------------- CUDA-graph replay of the same circuit
+    # MPSBatch.capture records every launch of the circuit once (device-resident,
+    # start state restored at the head of the graph); each replay is one launch
+    if not args.no_graph:
+        cap = aq.MPSBatch([aq.AdaptiveMPS(N_QUBITS, bond_dim=1, eps_bond=EPS, chi_max_per_bond=CHI, device=device,
+                                          device_resident=True)]).capture([ops_dev])
+        for _ in range(2):
+            cap.replay()
+        torch.cuda.synchronize()
+        g_ms = 0.0
+        for _ in range(args.steps):
+            flush_buf.zero_()
+            torch.cuda.synchronize()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(cap.stream)
+            cap.replay()
+            e.record(cap.stream)
+            e.synchronize()
+            g_ms += s.elapsed_time(e)
+        g_ms /= args.steps
+        cap.finish()
+        line["graph_replay"] = {"value": ngates / (g_ms / 1000.0), "unit": "gates/s", "ms_per_step": g_ms,
+                                "kernels_per_replay": cap.kernels_per_replay,
+                                "what": "the same circuit captured once (MPSBatch.capture) and replayed as one "
+                                        "CUDA graph: no host enqueue between layers"}
 
     # ---------------------------------------------------------------- FP64 reference state
     # this package's complex128 run (host-synchronised) of the same circuit

@@ -116,3 +116,24 @@ def test_single_qubit_batch_equals_sequential(dt):
     for m, ts in zip(insts, ref):
         for a, b in zip(m._tensors, ts):
             assert torch.equal(a, b)
+
+
+def test_config4_shaped_graph_batch_matches_fp64_oracle():
+    """The batched workload's shape at oracle-checkable sizes: hardware-efficient
+    ansatz instances of uneven qubit counts and chi caps, 10 layers, eps 1e-8,
+    device-resident and captured as one CUDA graph, each against the FP64
+    oracle run of that instance alone.  The caps equal 2^(n/2), so only eps
+    truncates and the float32 result stays within 1 - 1e-6 of FP64."""
+    specs = [(12, 64, 700), (14, 128, 701), (16, 256, 702)]
+    insts = [aq.AdaptiveMPS(n, bond_dim=1, eps_bond=1e-8, chi_max_per_bond=chi, device="cuda", device_resident=True)
+             for n, chi, _ in specs]
+    circs = [hea_circuit(n, 10, seed=sd) for n, _, sd in specs]
+    cap = aq.MPSBatch(insts).capture(circs)
+    cap.replay()
+    cap.finish()
+    for (n, chi, _), m, c in zip(specs, insts, circs):
+        o = mo.OracleMPS(n, bond_dim=1, eps_bond=1e-8, chi_max_per_bond=chi, dtype=np.complex128)
+        for kind, q, U in c:
+            (o.apply_two_site_gate if kind == "2q" else o.apply_single_qubit_gate)(q, U.numpy())
+        f = mo.mps_fidelity([t.cpu().numpy() for t in m.tensors], o.tensors)
+        assert f > 1 - 1e-6, (n, chi, f)
