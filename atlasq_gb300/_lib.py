@@ -70,6 +70,7 @@ _SIGS = {
     "agb_tune_tridiag_workspace": (SZ, [I, I, I]),
     "agb_tune_tridiag": (I, [I, I, I, P, SZ, P, P, P]),
     "agb_tuned_tridiag_cluster": (I, [I, I, I]),
+    "agb_set_tridiag_cluster": (I, [I, I, I, I, I]),
     "agb_set_tridiag_stages": (I, [I]),
     "agb_heevd_workspace": (SZ, [I, I, I]),
     "agb_heevd": (I, [I, I, I, I, P, P, P, P, SZ, U64, P]),

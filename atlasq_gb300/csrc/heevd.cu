@@ -5,6 +5,15 @@
 #include "prof.cuh"
 
 template <typename R> struct rlim;
+
+// Reciprocal of an LU pivot, the pivot first floored at piv in magnitude (a
+// zero pivot takes +piv).  The factors store reciprocals so that the back
+// substitution's dependent chain is multiply-adds only.
+template <typename R>
+__device__ __forceinline__ R inv_pivot(R u, R piv) {
+  if (fabs(u) < piv) u = copysign(piv, u == R(0) ? R(1) : u);
+  return R(1) / u;
+}
 template <> struct rlim<float> {
   static AGB_HD float eps() { return FLT_EPSILON; }
   static AGB_HD float pivmin() { return 1e-30f; }
@@ -324,14 +333,13 @@ __global__ void __launch_bounds__(128) invit_kernel(const HeevdProb* __restrict_
       pv = 1;
     }
     u2 = 0;
-    U0[i * L + t] = a0;
+    U0[i * L + t] = inv_pivot(a0, piv);
     U1[i * L + t] = a1;
     U2[i * L + t] = a2;
     Lm[i * L + t] = m;
     Pv[i * L + t] = pv;
   }
-  if (fabs(u0) < piv) u0 = copysign(piv, u0 == R(0) ? R(1) : u0);
-  U0[(int64_t)(n - 1) * L + t] = u0;
+  U0[(int64_t)(n - 1) * L + t] = inv_pivot(u0, piv);
   U1[(int64_t)(n - 1) * L + t] = 0;
   U2[(int64_t)(n - 1) * L + t] = 0;
   R* Y = (R*)P.Y;
@@ -402,9 +410,7 @@ __global__ void __launch_bounds__(128) invit_kernel(const HeevdProb* __restrict_
       for (int k = 0; k < IB; ++k) {
         const int i = i0 - k;
         if (i >= 0) {
-          R u = u0[k];
-          if (fabs(u) < piv) u = copysign(piv, u == R(0) ? R(1) : u);
-          const R x = (yb[k] - u1[k] * x1 - u2[k] * x2) / u;
+          const R x = (yb[k] - u1[k] * x1 - u2[k] * x2) * u0[k];  // u0: reciprocal pivot
           Y[(int64_t)i * L + t] = x;
           nrm += x * x;
           x2 = x1;
@@ -489,14 +495,13 @@ AGB_DEV void tri_lu(const R* d, const R* e, int n, R lam, R piv, R* U0, R* U1, R
       pv = 1;
     }
     u2 = 0;
-    U0[i * L + t] = a0;
+    U0[i * L + t] = inv_pivot(a0, piv);
     U1[i * L + t] = a1;
     U2[i * L + t] = a2;
     Lm[i * L + t] = m;
     Pv[i * L + t] = pv;
   }
-  if (fabs(u0) < piv) u0 = copysign(piv, u0 == R(0) ? R(1) : u0);
-  U0[(int64_t)(n - 1) * L + t] = u0;
+  U0[(int64_t)(n - 1) * L + t] = inv_pivot(u0, piv);
   U1[(int64_t)(n - 1) * L + t] = 0;
   U2[(int64_t)(n - 1) * L + t] = 0;
 }
@@ -554,9 +559,7 @@ AGB_DEV R tri_solve_pf(R* Y, int n, const R* U0, const R* U1, const R* U2, const
     for (int k = 0; k < IB; ++k) {
       const int i = i0 - k;
       if (i >= 0) {
-        R u = u0[k];
-        if (fabs(u) < piv) u = copysign(piv, u == R(0) ? R(1) : u);
-        const R x = (yb[k] - u1[k] * x1 - u2[k] * x2) / u;
+        const R x = (yb[k] - u1[k] * x1 - u2[k] * x2) * u0[k];  // u0: reciprocal pivot
         Y[(int64_t)i * L + t] = x;
         nrm += x * x;
         x2 = x1;

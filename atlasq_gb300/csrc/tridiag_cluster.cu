@@ -479,3 +479,18 @@ extern "C" int agb_tuned_tridiag_cluster(int dtype, int n, int count) {
   const int esz = dtype == AGB_C64 ? 8 : 16;
   return tridiag_cluster_size_for(esz, n, count);
 }
+
+extern "C" int agb_set_tridiag_cluster(int dtype, int n, int count, int C, int threads) {
+  if (dtype != AGB_C64 && dtype != AGB_C128) return AGB_ERR_ARG;
+  if (n <= 0 || n > 1024 || count <= 0 || C < 0 || C > 16 || (threads != 256 && threads != 512)) return AGB_ERR_ARG;
+  const int esz = dtype == AGB_C64 ? 8 : 16;
+  if (C > 0 && (C > n || !cluster_fits(esz, n, C))) return AGB_ERR_UNSUPPORTED;
+  if (C > tridiag_cluster_size(esz, n) && C > 8) {
+    // a non-portable size must be one the device schedules
+    const int maxC = esz == 8 ? max_cluster<float2>(kSmemBudget) : max_cluster<double2>(kSmemBudget);
+    if (C > maxC) return AGB_ERR_UNSUPPORTED;
+  }
+  g_tuned_C[esz == 16][(n + 31) / 32][count_class(count)] = C;
+  g_tuned_T[esz == 16][(n + 31) / 32][count_class(count)] = C > 0 ? threads : 0;
+  return AGB_OK;
+}

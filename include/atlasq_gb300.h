@@ -162,6 +162,11 @@ size_t agb_tune_tridiag_workspace(int dtype, int n, int count);
 int agb_tune_tridiag(int dtype, int n, int count, void* ws, size_t ws_bytes, void* stream, int* best_C,
                      float* best_ms);
 int agb_tuned_tridiag_cluster(int dtype, int n, int count);
+/* Set the cluster size C (1..16) and threads per CTA (256 or 512) the
+ * tridiagonalisation uses for this shape class, as agb_tune_tridiag would;
+ * C = 0 restores the built-in choice.  AGB_ERR_UNSUPPORTED if the matrix does
+ * not fit that cluster. */
+int agb_set_tridiag_cluster(int dtype, int n, int count, int C, int threads);
 
 /* Tridiagonalisation used by the eigensolver: 0 the two-stage reduction
  * (dense -> band of width 16 or 8 on a thread-block cluster, then bulge
