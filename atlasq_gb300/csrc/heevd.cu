@@ -1054,7 +1054,11 @@ __global__ void __launch_bounds__(WARPS * 32) backtransform2_kernel(const HeevdP
 
 template <typename CX, int NK>
 int launch_bt(const HeevdProb* probs, int count, int maxell, cudaStream_t s) {
-  constexpr int WARPS = (sizeof(CX) * NK > 128) ? 8 : 16;
+  // 4 warps (8 columns) per CTA: a saturated headline layer then has 32 CTAs
+  // per large problem instead of 8, so the large problems' work spreads over
+  // every SM rather than the ~96 their CTAs covered while the small problems'
+  // SMs idled (each CTA stages every reflector pair once; the extra reads hit L2).
+  constexpr int WARPS = 4;
   constexpr size_t smem = (size_t)4 * NK * 32 * sizeof(CX);
   const cudaError_t oe = agb_smem_optin(backtransform2_kernel<CX, NK, WARPS>, smem);
   if (oe != cudaSuccess) {
