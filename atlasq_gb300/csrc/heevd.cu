@@ -570,6 +570,167 @@ AGB_DEV R tri_solve_pf(R* Y, int n, const R* U0, const R* U1, const R* U2, const
   return nrm;
 }
 
+// Inverse iteration, complex64 path (float tridiagonal), for n <= 1024: the
+// same LU, start vectors and three solves as invit_kernel, with the iterate of
+// each thread's eigenvector kept in shared memory and the LU factors streamed
+// from L2 through a per-thread ring of cp.async copies issued AHEAD chunks of
+// CH steps before use.  The solves' recurrences are chains of multiply-adds
+// (reciprocal pivots), so with the operands already in shared memory a step
+// costs a few cycles instead of an L2 round trip every IB steps.  Each thread
+// reads only its own ring entries and its own iterate column: no block-level
+// synchronisation after the tridiagonal is staged.  TB threads per CTA.
+__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+constexpr int kInvCH = 16, kInvNCH = 6;  // steps per chunk, chunks in the ring (5 in flight)
+
+size_t invit_async_smem(int n, int tb) {
+  return ((size_t)2 * n + (size_t)n * tb + (size_t)3 * kInvNCH * kInvCH * tb) * sizeof(float);
+}
+
+template <int TB>
+__global__ void __launch_bounds__(TB) invit_async_kernel(const HeevdProb* __restrict__ probs) {
+  constexpr int CH = kInvCH, NCH = kInvNCH, RS = NCH * CH;  // ring steps per array
+  typedef float R;
+  const HeevdProb P = probs[blockIdx.y];
+  const int n = P.n, ell = P.ell, nv = P.nvec;
+  if (blockIdx.x * TB >= nv || P.skip_vectors) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  R* d = (R*)smem_raw;            // [n]
+  R* e = d + n;                   // [n]
+  R* ys = e + n;                  // [n][TB] iterate column of each thread
+  R* ring = ys + (size_t)n * TB;  // [3][RS][TB] streamed factors
+  for (int i = threadIdx.x; i < n; i += TB) {
+    d[i] = ((const R*)P.d)[i];
+    e[i] = (i < n - 1) ? ((const R*)P.e)[i] : R(0);
+  }
+  __syncthreads();  // the last block-level barrier: threads may leave from here on
+  const int tid = threadIdx.x, t = blockIdx.x * TB + tid;
+  if (t >= nv) return;
+  if (in_cluster((const R*)P.lam, nv, t, cluster_tol((const R*)P.lam, ell, P.ctol))) return;
+  const R lam = ((const R*)P.lam)[t];
+  R tnorm = 0;
+  for (int i = 0; i < n; ++i) tnorm = fmax(tnorm, fabs(d[i]) + fabs(e[i]) + (i ? fabs(e[i - 1]) : R(0)));
+  const R piv = rlim<R>::eps() * fmax(tnorm, rlim<R>::pivmin());
+  R* lu = (R*)P.lu;
+  const int64_t L = ell;
+  R* U0 = lu;
+  R* U1 = lu + (int64_t)n * L;
+  R* U2 = lu + 2 * (int64_t)n * L;
+  R* Lm = lu + 3 * (int64_t)n * L;
+  R* Pv = lu + 4 * (int64_t)n * L;
+  tri_lu(d, e, n, lam, piv, U0, U1, U2, Lm, Pv, L, t);
+  __threadfence_block();  // the factor stores precede the copies that read them back
+  // start vector: uniform in [-1, 1), four entries per Philox call (a Gaussian
+  // start costs a Philox call plus Box-Muller per entry, half of this kernel's
+  // instructions; inverse iteration only needs a start with a component along
+  // the wanted vector)
+  R nrm = 0;
+  const uint64_t per = (uint64_t)((n + 3) / 4);
+  for (int i0 = 0; i0 < n; i0 += 4) {
+    const uint64_t idx = (uint64_t)t * per + (uint64_t)(i0 >> 2);
+    const philox_out o = philox4x32_10((uint32_t)idx, (uint32_t)(idx >> 32), 0x11u, 0x5EEDu, (uint32_t)P.seed,
+                                       (uint32_t)(P.seed >> 32));
+    const uint32_t w[4] = {o.x, o.y, o.z, o.w};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int i = i0 + k;
+      if (i < n) {
+        const R b = (R)(int32_t)w[k] * R(4.656612873077393e-10);  // 2^-31
+        ys[i * TB + tid] = b;
+        nrm += b * b;
+      }
+    }
+  }
+  auto rg = [&](int a, int step) -> R* { return ring + ((size_t)a * RS + step % RS) * TB + tid; };
+  const int nf = n - 1;  // forward steps i = 0 .. n-2 (operands Pv[i], Lm[i])
+  auto issue_f = [&](int c) {
+    for (int k = 0; k < CH; ++k) {
+      const int i = c * CH + k;
+      if (i < nf) {
+        cp_async4(rg(0, i), Pv + (int64_t)i * L + t);
+        cp_async4(rg(1, i), Lm + (int64_t)i * L + t);
+      }
+    }
+    cp_async_commit();
+  };
+  // backward steps j = 0 .. n-1 handle row i = n-1-j (operands U0, U1, U2 of row i)
+  auto issue_b = [&](int c) {
+    for (int k = 0; k < CH; ++k) {
+      const int j = c * CH + k;
+      if (j < n) {
+        const int i = n - 1 - j;
+        cp_async4(rg(0, j), U0 + (int64_t)i * L + t);
+        cp_async4(rg(1, j), U1 + (int64_t)i * L + t);
+        cp_async4(rg(2, j), U2 + (int64_t)i * L + t);
+      }
+    }
+    cp_async_commit();
+  };
+  const int cf = (nf + CH - 1) / CH, cb = (n + CH - 1) / CH;
+  for (int it = 0; it < 3; ++it) {
+    const R s = R(1) / sqrt(fmax(nrm, rlim<R>::pivmin()));
+    // forward: apply P and L
+    for (int c = 0; c < NCH - 1; ++c) issue_f(c);
+    R bi = ys[tid] * s;
+    for (int c = 0; c < cf; ++c) {
+      issue_f(c + NCH - 1);  // an empty group past the end keeps the count uniform
+      cp_async_wait<NCH - 1>();  // chunk c has landed
+#pragma unroll 4
+      for (int k = 0; k < CH; ++k) {
+        const int i = c * CH + k;
+        if (i < nf) {
+          R bn = ys[(i + 1) * TB + tid] * s;
+          if (*rg(0, i) != R(0)) {
+            const R tmp = bi;
+            bi = bn;
+            bn = tmp;
+          }
+          ys[i * TB + tid] = bi;
+          bi = bn - *rg(1, i) * bi;
+        }
+      }
+    }
+    ys[(n - 1) * TB + tid] = bi;
+    cp_async_wait<0>();  // no copy in flight into the ring before it is reused
+    // backward substitution with the reciprocal pivots
+    for (int c = 0; c < NCH - 1; ++c) issue_b(c);
+    R x1 = 0, x2 = 0;
+    nrm = 0;
+    for (int c = 0; c < cb; ++c) {
+      issue_b(c + NCH - 1);
+      cp_async_wait<NCH - 1>();
+#pragma unroll 4
+      for (int k = 0; k < CH; ++k) {
+        const int j = c * CH + k;
+        if (j < n) {
+          const int i = n - 1 - j;
+          const R x = (ys[i * TB + tid] - *rg(1, j) * x1 - *rg(2, j) * x2) * *rg(0, j);
+          ys[i * TB + tid] = x;
+          nrm += x * x;
+          x2 = x1;
+          x1 = x;
+        }
+      }
+    }
+    cp_async_wait<0>();
+    if (!(nrm < R(1e300)) || !(nrm > R(0))) {  // overflow / breakdown: restart from a unit vector
+      for (int i = 0; i < n; ++i) ys[i * TB + tid] = (i == (t % n)) ? R(1) : R(0);
+      nrm = 1;
+    }
+  }
+  const R sc = R(1) / sqrt(fmax(nrm, rlim<R>::pivmin()));
+  R* Y = (R*)P.Y;
+  for (int i = 0; i < n; ++i) Y[(int64_t)i * L + t] = ys[i * TB + tid] * sc;
+}
+
 // CGS2 of column jj of the staged cluster block Z (n x c, row-major in shared
 // memory) against its columns [0, jj), then normalisation (block-wide).
 template <typename R>
@@ -1120,7 +1281,23 @@ int launch_heevd_vectors(HeevdProb* probs, GemmProb* gp, int count, int maxn, in
   if (count <= 0 || maxn <= 0 || maxell <= 0) return AGB_OK;
   const size_t sm_r = 2 * (size_t)maxn * sizeof(R);
   prof_mark(AGB_ST_INVIT, s);
-  invit_kernel<R><<<dim3((maxell + 127) / 128, count), 128, sm_r, s>>>(probs);
+  if (sizeof(R) == 4 && maxn <= 1024) {
+    // complex64: iterate in shared memory, factors streamed by cp.async
+    const int tb = maxn <= 512 ? 64 : 32;
+    const size_t sm = invit_async_smem(maxn, tb);
+    const cudaError_t oe = tb == 64 ? agb_smem_optin(invit_async_kernel<64>, sm)
+                                    : agb_smem_optin(invit_async_kernel<32>, sm);
+    if (oe != cudaSuccess) {
+      agb_note_error(__FILE__, __LINE__, oe);
+      return AGB_ERR_CUDA;
+    }
+    if (tb == 64)
+      invit_async_kernel<64><<<dim3((maxell + 63) / 64, count), 64, sm, s>>>(probs);
+    else
+      invit_async_kernel<32><<<dim3((maxell + 31) / 32, count), 32, sm, s>>>(probs);
+  } else {
+    invit_kernel<R><<<dim3((maxell + 127) / 128, count), 128, sm_r, s>>>(probs);
+  }
   AGB_CHECK_LAUNCH();
   prof_mark(AGB_ST_CLUSTER, s);
   {
