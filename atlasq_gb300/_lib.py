@@ -94,6 +94,7 @@ _SIGS = {
     "agb_mlp_adam": (I, [P, P, P, P, I, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                          ctypes.c_float, P]),
     "agb_cgemm_tc_workspace": (SZ, [I, I, I, I]),
+    "agb_set_gemm_wait_limit": (I, [ctypes.c_longlong]),
     "agb_cgemm_tc": (I, [ctypes.c_char, ctypes.c_char, I, I, I, I, P, I64, I64, P, I64, I64, P, I64, I64,
                          ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, P, SZ, P, P]),
     "agb_cgemm_tc_async": (I, [ctypes.c_char, ctypes.c_char, I, I, I, I, P, I64, I64, P, I64, I64, P, I64, I64,

@@ -53,10 +53,10 @@ AGB_DEV void mbar_init(uint64_t* bar, uint32_t count) {
 AGB_DEV void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
-// true when phase `parity` of the barrier completed; false after WAIT_LIMIT polls
-AGB_DEV bool mbar_wait(uint64_t* bar, uint32_t parity) {
+// true when phase `parity` of the barrier completed; false after `limit` polls
+AGB_DEV bool mbar_wait(uint64_t* bar, uint32_t parity, unsigned limit = WAIT_LIMIT) {
   const uint32_t a = smem_u32(bar);
-  for (unsigned it = 0; it < WAIT_LIMIT; ++it) {
+  for (unsigned it = 0; it < limit; ++it) {
     uint32_t ok;
     asm volatile(
         "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n}\n"
@@ -206,7 +206,7 @@ AGB_DEV void store_slice(const Operand& o, uint32_t tile, int plane_bytes, int c
 
 // ------------------------------------------------------------------ GEMM
 __global__ void __launch_bounds__(NTHREADS, 1)
-    tc_gemm_kernel(const GemmProb* __restrict__ probs, int* __restrict__ status) {
+    tc_gemm_kernel(const GemmProb* __restrict__ probs, int* __restrict__ status, unsigned pipe_limit) {
   const GemmProb P = probs[blockIdx.z];
   const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
   if (m0 >= P.M || n0 >= P.N) return;
@@ -246,7 +246,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       float2 va[4 * QA], vb[4 * QB];
       load_slice<QA>(oa, m0, kt * BK, ct, va);  // in flight while the stage drains
       load_slice<QB>(ob, n0, kt * BK, ct, vb);
-      if (kt >= STAGES && !mbar_wait(&empty[s], ((kt / STAGES) - 1) & 1)) {
+      if (kt >= STAGES && !mbar_wait(&empty[s], ((kt / STAGES) - 1) & 1, pipe_limit)) {
         *abort_flag = 1;
         break;
       }
@@ -265,7 +265,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     for (int kt = 0; kt < nk; ++kt) {
       const int s = kt % STAGES;
       const uint32_t d_re = tmem + (uint32_t)(2 * BN * (kt % NACC)), d_im = d_re + BN;
-      if (!mbar_wait(&full[s], (kt / STAGES) & 1)) {
+      if (!mbar_wait(&full[s], (kt / STAGES) & 1, pipe_limit)) {
         *abort_flag = 1;
         break;
       }
@@ -302,7 +302,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     umma_commit(done);  // every MMA issued above has completed when this arrives
   }
   __syncwarp();
-  // ---------------- epilogue (warps 0-7); the MMA warp waits for the MMAs before freeing TMEM
+  // ---------------- epilogue (warps 0-7); the MMA warp waits for the MMAs before freeing TMEM.
+  // This wait keeps the full limit even when the pipeline's is lowered, so an
+  // aborted tile still retires every MMA it issued before TMEM is freed.
   const bool ok = mbar_wait(done, 0);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (warp < CONV_WARPS && ok && !*abort_flag) {
@@ -361,7 +363,17 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 
 int round_up(int x, int m) { return (x + m - 1) / m * m; }
 
+unsigned g_pipe_limit = WAIT_LIMIT;
+
 }  // namespace
+
+// Poll limit of the GEMM's pipeline waits (stage full / empty); a negative value
+// restores the default.  Lets a test make those waits expire: the kernel then
+// reports AGB_ERR_TIMEOUT and skips its epilogue.
+extern "C" int agb_set_gemm_wait_limit(long long polls) {
+  g_pipe_limit = polls < 0 ? WAIT_LIMIT : (unsigned)(polls < (long long)WAIT_LIMIT ? polls : (long long)WAIT_LIMIT);
+  return AGB_OK;
+}
 
 // The split operands live only in shared memory: the tensor-core path needs
 // no global scratch beyond a token the dispatcher checks for.
@@ -386,7 +398,7 @@ int launch_gemm_tc(const GemmProb* probs, int count, int maxM, int maxN, int max
       return AGB_ERR_CUDA;
     attr = true;
   }
-  tc_gemm_kernel<<<dim3(Np / BN, Mp / BM, count), NTHREADS, SMEM_BYTES, s>>>(probs, status);
+  tc_gemm_kernel<<<dim3(Np / BN, Mp / BM, count), NTHREADS, SMEM_BYTES, s>>>(probs, status, g_pipe_limit);
   AGB_CHECK_LAUNCH();
   return AGB_OK;
 }

@@ -304,6 +304,13 @@ int agb_cgemm_tc_async(char opA, char opB, int batch, int M, int N, int K, const
                        int64_t strideC, float alpha_re, float alpha_im, float beta_re, float beta_im, void* ws,
                        size_t ws_bytes, int* status_dev, void* stream);
 
+/* Poll limit of the tensor-core GEMM's pipeline waits (process-wide; a negative
+ * value restores the default of 2^26 polls).  A test hook with no reference
+ * counterpart: at 0 the waits expire at once, the kernel records
+ * AGB_ERR_TIMEOUT, waits (full limit) for the MMAs it issued, frees its tensor
+ * memory and returns; the context stays usable. */
+int agb_set_gemm_wait_limit(long long polls);
+
 /* Batched complex GEMM (SIMT reference-free kernel, used by the host layer):
  * C[b] = alpha * op(A[b]) op(B[b]) + beta * C[b]; op: 'N' (as stored), 'T' (transposed),
  * 'C' (conjugate-transposed), 'R' (conjugated, not transposed). */

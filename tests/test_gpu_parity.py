@@ -84,6 +84,51 @@ def test_cgemm_tensor_cores_3xtf32(opA, opB, M, N, K, batch):
     assert rel(C, ref) < 1e-6 + 2e-9 * K
 
 
+def test_cgemm_tensor_cores_bounded_wait_expires_cleanly():
+    """The GEMM's pipeline waits are bounded.  With their poll limit set to 0 no
+    stage can be waited for, so every tile aborts: the synchronous entry returns
+    AGB_ERR_TIMEOUT, the asynchronous one sets the device status word, which
+    stays set through a later successful call; the context stays usable and the
+    next call with the default limit is correct."""
+    import ctypes
+    from atlasq_gb300 import _lib
+    lib = _lib.load()
+    g = torch.Generator().manual_seed(5)
+    A = crandn(2, 256, 96, gen=g).to(DEV)
+    B = crandn(2, 96, 128, gen=g).to(DEV)
+    bat, M, K, N = 2, 256, 96, 128
+    C = torch.zeros(bat, M, N, dtype=torch.complex64, device=DEV)
+    need = lib.agb_cgemm_tc_workspace(bat, M, N, K)
+    ws = torch.empty(need, dtype=torch.uint8, device=DEV)
+    stream = torch.cuda.current_stream().cuda_stream
+    word = torch.zeros(1, dtype=torch.int32, device=DEV)
+
+    def call(status_host=None, status_dev=None):
+        args = (b"N", b"N", bat, M, N, K, A.data_ptr(), K, M * K, B.data_ptr(), N, K * N, C.data_ptr(), N, M * N,
+                1.0, 0.0, 0.0, 0.0, ws.data_ptr(), need)
+        if status_dev is None:
+            return lib.agb_cgemm_tc(*args, ctypes.byref(status_host), stream)
+        return lib.agb_cgemm_tc_async(*args, status_dev.data_ptr(), stream)
+
+    assert lib.agb_set_gemm_wait_limit(0) == 0
+    try:
+        st = ctypes.c_int(0)
+        assert call(status_host=st) == _lib.AGB_ERR_TIMEOUT
+        assert st.value == _lib.AGB_ERR_TIMEOUT
+        assert call(status_dev=word) == 0
+        torch.cuda.synchronize()
+        assert int(word.item()) == _lib.AGB_ERR_TIMEOUT
+    finally:
+        lib.agb_set_gemm_wait_limit(-1)
+    st = ctypes.c_int(0)
+    assert call(status_host=st) == 0 and st.value == 0
+    ref = A.cpu().numpy().astype(np.complex128) @ B.cpu().numpy().astype(np.complex128)
+    assert rel(C.cpu().numpy(), ref) < 1e-6
+    assert call(status_dev=word) == 0
+    torch.cuda.synchronize()
+    assert int(word.item()) == _lib.AGB_ERR_TIMEOUT  # sticky: never cleared by the library
+
+
 @functools.lru_cache(maxsize=1)
 def _hermitian_cases():
     g = torch.Generator().manual_seed(11)

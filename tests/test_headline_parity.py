@@ -4,7 +4,9 @@ tests/golden/make_golden.py (``brickwork_n40_d20_chi256.npz``):
 
 * first 150 gates, before the chi cap truncates anything the float32 rule
   can see: the kept rank of every gate equal to the reference's complex64
-  choice up to the spread of the reference's own two precisions (minimum 2).
+  choice up to the spread of the reference's own two precisions (minimum 2),
+  or further where the singular values between the two ranks carry less
+  than one float32 ulp of the total weight (a cut decided by rounding).
   At eps 1e-8 the float32 rule keeps values until the float32 cumulative sum
   stops changing, so the rank is decided by trailing values at ~1e-7 of the
   total, where two float32 SVDs differ: the reference keeps 63 vs 64 (gate
@@ -63,8 +65,22 @@ def test_headline_first_150_gates_match_reference():
     logs = m.statistics.logs
     ref_sv = unpack_spectra(g["sv_lens"], g["sv_flat"])
     k64, k128 = [int(x) for x in g["k64"][:pinned]], [int(x) for x in g["k128"][:pinned]]
+    # A kept rank may differ from the reference's complex64 run by more than the
+    # reference's own complex64 / complex128 spread only where the weight of
+    # the singular values between the two ranks is below one float32 ulp of the
+    # total: the rule's float32 cumulative sum decides such a cut by rounding
+    # alone (with eps_bond = 1e-8 the sum must reach the float32 total).
+    def rounding_edge(j, k, a):
+        ref = ref_sv[j].astype(np.float64)
+        if k < a:
+            between = np.sum(ref[k:a] ** 2)
+        else:
+            sig = np.asarray(m.spectrum_log[j][2], np.float64)
+            between = np.sum(sig[a:k] ** 2)
+        return between <= 2.0 ** -23 * np.sum(ref ** 2)
+
     bad = [(j, k, a, b) for j, (k, a, b) in enumerate(zip(logs["k_star"], k64, k128))
-           if abs(k - a) > max(abs(b - a), 2)]
+           if abs(k - a) > max(abs(b - a), 2) and not rounding_edge(j, k, a)]
     assert not bad, bad
     assert sum(k != a for k, a in zip(logs["k_star"], k64)) <= 5  # float32 edge cases only
     assert len(m.spectrum_log) == pinned
