@@ -25,6 +25,8 @@
 // are read and written only by their owning CTA, between block barriers.
 #include <cooperative_groups.h>
 
+#include <type_traits>
+
 #include "heevd.cuh"
 #include "prof.cuh"
 
@@ -165,25 +167,33 @@ __global__ void __launch_bounds__(512, 1) tridiag_cluster_kernel(const HeevdProb
     // step to columns > j and accumulate sum_{c <= r} A[r][c] v_c.
     {
       const int i0 = (j + 1 - q + C - 1) / C > 0 ? (j + 1 - q + C - 1) / C : 0;
-      for (int i = i0 + wid; i < nown; i += nw) {
-        const int r = q + i * C;
-        CX* row = rowp(i);
-        const CX vr = vprev[r], wr = wprev[r];
-        CX acc = czero<CX>();
-        for (int c = j + 1 + lane; c <= r; c += 32) {
-          CX a = row[c];
-          if (prev_active) {  // column j itself was updated at the end of the previous step
-            a = csub(a, cmul(vr, cconj(wprev[c])));
-            a = csub(a, cmul(wr, cconj(vprev[c])));
-            row[c] = a;
+      // the four (update, matvec) cases as separate loops: no per-element branch
+      auto row_pass = [&](auto upd, auto mv) {
+        for (int i = i0 + wid; i < nown; i += nw) {
+          const int r = q + i * C;
+          CX* row = rowp(i);
+          const CX vr = vprev[r], wr = wprev[r];
+          CX acc = czero<CX>();
+          for (int c = j + 1 + lane; c <= r; c += 32) {
+            CX a = row[c];
+            if constexpr (decltype(upd)::value) {  // column j itself was updated at the end of the previous step
+              a = csub(a, cmul(vr, cconj(wprev[c])));
+              a = csub(a, cmul(wr, cconj(vprev[c])));
+              row[c] = a;
+            }
+            if constexpr (decltype(mv)::value) cfma(acc, a, v[c]);
           }
-          if (active) cfma(acc, a, v[c]);
+          if constexpr (decltype(mv)::value) {
+            acc = warp_csum(acc);
+            if (lane == 0) pp[r] = acc;  // rows are owned by one warp: plain store
+          }
         }
-        if (active) {
-          acc = warp_csum(acc);
-          if (lane == 0) pp[r] = acc;  // rows are owned by one warp: plain store
-        }
-      }
+      };
+      using T_ = std::true_type;
+      using F_ = std::false_type;
+      if (prev_active && active) row_pass(T_{}, T_{});
+      else if (active) row_pass(F_{}, T_{});
+      else if (prev_active) row_pass(T_{}, F_{});
       __syncthreads();
       // Column pass (thread per column): the strictly-lower entries of the own
       // rows contribute conj(A[r][c]) v_r to p[c] through Hermitian symmetry.
@@ -192,9 +202,23 @@ __global__ void __launch_bounds__(512, 1) tridiag_cluster_kernel(const HeevdProb
         for (int c = j + 1 + tid; c < n; c += nt) {
           const int ic = (c + 1 - q + C - 1) / C > 0 ? (c + 1 - q + C - 1) / C : 0;  // own rows r > c
           CX acc = czero<CX>();
-          for (int i = (ic > i0 ? ic : i0); i < nown; ++i) {
-            const int r = q + i * C;
-            cfma(acc, cconj(rowp(i)[c]), v[r]);
+          int i = ic > i0 ? ic : i0;
+          if constexpr (!OVERFLOW) {
+            // walk the packed rows: offset(i + 1) - offset(i) = q + 1 + C i
+            const CX* a = rows + row_offset(i, q, C) + c;
+            const CX* vr = v + q + i * C;
+            int stride = q + 1 + C * i;
+            for (; i < nown; ++i) {
+              cfma(acc, cconj(*a), *vr);
+              a += stride;
+              stride += C;
+              vr += C;
+            }
+          } else {
+            for (; i < nown; ++i) {
+              const int r = q + i * C;
+              cfma(acc, cconj(rowp(i)[c]), v[r]);
+            }
           }
           pp[c] = cadd(pp[c], acc);
         }
