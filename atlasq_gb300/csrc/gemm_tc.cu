@@ -6,16 +6,20 @@
 //    and op(B)^T (64 x 32) straight from the operands with coalesced loads
 //    (along k when k is contiguous in memory, along the rows otherwise), split
 //    each value into TF32 hi = x rounded to TF32 (11-bit significand) and
-//    lo = x - hi, fold conjugation into the imaginary parts, and store the
-//    eight planes {Re_hi, Re_lo, Im_hi, Im_lo} x {A, B} into a shared-memory
-//    stage in the K-major 128-byte-swizzled layout the tensor core reads
-//    (the layout a TMA SWIZZLE_128B copy of 32-float rows produces);
-//    out-of-range rows and k are stored as zeros;
-//  * warp 8 lane 0 issues tcgen05.mma.kind::tf32 (M=128, N=64, K=8) per stage:
-//       Re += Ar_h Br_h + Ar_h Br_l + Ar_l Br_h - (Ai_h Bi_h + Ai_h Bi_l + Ai_l Bi_h)
-//       Im += Ar_h Bi_h + Ar_h Bi_l + Ar_l Bi_h +  Ai_h Br_h + Ai_h Br_l + Ai_l Br_h
-//    into fp32 accumulators in tensor memory (the minus sign is the
-//    instruction descriptor's negate-A bit), k slices rotating over four
+//    lo = x - hi, fold conjugation into the imaginary parts, and store them
+//    into a shared-memory stage in the K-major 128-byte-swizzled layout the
+//    tensor core reads (the layout a TMA SWIZZLE_128B copy of 32-float rows
+//    produces): A as four planes {Re_hi, Re_lo, Im_hi, Im_lo}, B as two
+//    planes {hi, lo} of 192 rows [-Im | Re | Im]; out-of-range rows and k are
+//    stored as zeros;
+//  * warp 8 lane 0 issues tcgen05.mma.kind::tf32 (M=128, N=128, K=8) per stage,
+//    the real and imaginary accumulators of the tile being adjacent TMEM
+//    columns written by one MMA: with B rows 64..191 = [Re | Im] and rows
+//    0..127 = [-Im | Re],
+//       [Re | Im] += Ar_h [Br|Bi]_h + Ar_h [Br|Bi]_l + Ar_l [Br|Bi]_h
+//                  + Ai_h [-Bi|Br]_h + Ai_h [-Bi|Br]_l + Ai_l [-Bi|Br]_h
+//    (six MMAs per K=8 step, each accumulator receiving the same products in
+//    the same order as twelve N=64 MMAs would), k slices rotating over four
 //    accumulator pairs; a commit per stage frees the stage for the converters;
 //  * warps 0-7 then read the accumulators with tcgen05.ld (warp w reads TMEM
 //    lanes 32(w%4)..+31 = tile rows, columns 32(w/4)..+31) and write
@@ -33,8 +37,9 @@ namespace {
 
 constexpr int BM = 128, BN = 64, BK = 32, STAGES = 2;
 constexpr int TILE_A = BM * BK * 4;                    // 16 KiB per plane
-constexpr int TILE_B = BN * BK * 4;                    // 8 KiB per plane
-constexpr int STAGE_BYTES = 4 * TILE_A + 4 * TILE_B;   // 96 KiB
+constexpr int B_ROWS = 3 * BN;                         // B plane rows: -Im | Re | Im
+constexpr int TILE_B = B_ROWS * BK * 4;                // 24 KiB per plane (hi, lo)
+constexpr int STAGE_BYTES = 4 * TILE_A + 2 * TILE_B;   // 112 KiB
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
 constexpr int NACC = 4;                                // k-tiles rotate over 4 accumulator pairs
 constexpr int TMEM_COLS = 2 * BN * NACC;               // 512 columns: (Re, Im) x 4
@@ -78,9 +83,11 @@ AGB_DEV uint64_t sdesc(uint32_t saddr) {
   d |= (uint64_t)2 << 61;             // SWIZZLE_128B
   return d;
 }
-// Instruction descriptor, kind::tf32: D f32, A/B tf32, K-major, M=128, N=64.
-constexpr uint32_t IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
-constexpr uint32_t NEG_A = 1u << 13;
+// Instruction descriptor, kind::tf32: D f32, A/B tf32, K-major, M=128, N=128
+// (the real and imaginary accumulators of a tile are adjacent TMEM columns,
+// written by one MMA).
+constexpr uint32_t IDESC =
+    (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)((2 * BN) >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
 
 AGB_DEV void umma(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
   asm volatile(
@@ -181,6 +188,35 @@ AGB_DEV void load_slice(const Operand& o, int r0, int k0, int ct, float2* v) {
     }
   }
 }
+// B quads: the hi and lo planes hold rows [-Im | Re | Im] (BN rows each), so
+// rows BN..3BN-1 are the operand [Re | Im] of an A_re product and rows
+// 0..2BN-1 the operand [-Im | Re] of an A_im product: one N = 2 BN MMA then
+// accumulates both the real and the imaginary part of the tile.
+template <int NQ>
+AGB_DEV void store_slice_b(const Operand& o, uint32_t tile, int ct, const float2* v) {
+#pragma unroll
+  for (int j = 0; j < NQ; ++j) {
+    int r, k4;
+    quad_coord(o.k_contig, ct, j, r, k4);
+    float rh[4], rl[4], ih[4], il[4];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      const float re = v[4 * j + t].x, im = o.conj ? -v[4 * j + t].y : v[4 * j + t].y;
+      rh[t] = tf32_hi(re);
+      ih[t] = tf32_hi(im);
+      rl[t] = re - rh[t];
+      il[t] = im - ih[t];
+    }
+    const uint32_t a = tile + sw128(r, k4);  // rows r, r + BN, r + 2 BN share the swizzle phase
+    constexpr uint32_t RB = BN * 128;
+    st_shared_v4(a, -ih[0], -ih[1], -ih[2], -ih[3]);
+    st_shared_v4(a + RB, rh[0], rh[1], rh[2], rh[3]);
+    st_shared_v4(a + 2 * RB, ih[0], ih[1], ih[2], ih[3]);
+    st_shared_v4(a + TILE_B, -il[0], -il[1], -il[2], -il[3]);
+    st_shared_v4(a + TILE_B + RB, rl[0], rl[1], rl[2], rl[3]);
+    st_shared_v4(a + TILE_B + 2 * RB, il[0], il[1], il[2], il[3]);
+  }
+}
 template <int NQ>
 AGB_DEV void store_slice(const Operand& o, uint32_t tile, int plane_bytes, int ct, const float2* v) {
 #pragma unroll
@@ -253,7 +289,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       if (*abort_flag) break;
       const uint32_t st = smem_u32(smem + s * STAGE_BYTES);
       store_slice<QA>(oa, st, TILE_A, ct, va);
-      store_slice<QB>(ob, st + 4 * TILE_A, TILE_B, ct, vb);
+      store_slice_b<QB>(ob, st + 4 * TILE_A, ct, vb);
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // visible to the tensor core
       mbar_arrive(&full[s]);
     }
@@ -264,7 +300,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     // the chain length); the epilogue sums the pairs in fp32.
     for (int kt = 0; kt < nk; ++kt) {
       const int s = kt % STAGES;
-      const uint32_t d_re = tmem + (uint32_t)(2 * BN * (kt % NACC)), d_im = d_re + BN;
+      const uint32_t d = tmem + (uint32_t)(2 * BN * (kt % NACC));  // [re | im] columns of pair kt % NACC
       if (!mbar_wait(&full[s], (kt / STAGES) & 1, pipe_limit)) {
         *abort_flag = 1;
         break;
@@ -275,27 +311,22 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       const uint32_t sb = sa + 4 * TILE_A;
 #pragma unroll
       for (int ks = 0; ks < BK / 8; ++ks) {
-        uint64_t a[4], bb[4];
+        uint64_t a[4];
 #pragma unroll
-        for (int pl = 0; pl < 4; ++pl) {
-          a[pl] = sdesc(sa + pl * TILE_A) + (uint64_t)(ks * 2);   // +32 bytes per K=8 step
-          bb[pl] = sdesc(sb + pl * TILE_B) + (uint64_t)(ks * 2);
-        }
+        for (int pl = 0; pl < 4; ++pl) a[pl] = sdesc(sa + pl * TILE_A) + (uint64_t)(ks * 2);  // +32 bytes per K=8 step
+        // [Re | Im] and [-Im | Re] windows of the hi and lo B planes
+        const uint64_t bre_hi = sdesc(sb + BN * 128) + (uint64_t)(ks * 2);
+        const uint64_t bre_lo = sdesc(sb + TILE_B + BN * 128) + (uint64_t)(ks * 2);
+        const uint64_t bim_hi = sdesc(sb) + (uint64_t)(ks * 2);
+        const uint64_t bim_lo = sdesc(sb + TILE_B) + (uint64_t)(ks * 2);
         const uint32_t first = (kt < NACC && ks == 0) ? 0u : 1u;
-        // real part
-        umma(d_re, a[0], bb[0], IDESC, first);
-        umma(d_re, a[0], bb[1], IDESC, 1);
-        umma(d_re, a[1], bb[0], IDESC, 1);
-        umma(d_re, a[2], bb[2], IDESC | NEG_A, 1);
-        umma(d_re, a[2], bb[3], IDESC | NEG_A, 1);
-        umma(d_re, a[3], bb[2], IDESC | NEG_A, 1);
-        // imaginary part
-        umma(d_im, a[0], bb[2], IDESC, first);
-        umma(d_im, a[0], bb[3], IDESC, 1);
-        umma(d_im, a[1], bb[2], IDESC, 1);
-        umma(d_im, a[2], bb[0], IDESC, 1);
-        umma(d_im, a[2], bb[1], IDESC, 1);
-        umma(d_im, a[3], bb[0], IDESC, 1);
+        // re += Are Bre - Aim Bim,  im += Are Bim + Aim Bre  (3xTF32: hi hi, hi lo, lo hi)
+        umma(d, a[0], bre_hi, IDESC, first);
+        umma(d, a[0], bre_lo, IDESC, 1);
+        umma(d, a[1], bre_hi, IDESC, 1);
+        umma(d, a[2], bim_hi, IDESC, 1);
+        umma(d, a[2], bim_lo, IDESC, 1);
+        umma(d, a[3], bim_hi, IDESC, 1);
       }
       umma_commit(&empty[s]);  // stage s may be refilled once these MMAs retire
     }
