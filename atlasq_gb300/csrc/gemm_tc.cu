@@ -298,6 +298,13 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     // k-tile kt accumulates into pair kt % NACC: four chains of length K/4 instead
     // of one of length K (the tensor core's fp32 accumulation error grows with
     // the chain length); the epilogue sums the pairs in fp32.
+    // Shared-memory descriptors: the address field is (address / 16) in the low
+    // 14 bits, so a descriptor at a 16-byte multiple `off` past a stage base is
+    // the base's descriptor + off / 16 (every operand lies below 256 KiB); the
+    // two stage bases are formed once.
+    static_assert(STAGES == 2, "two stage descriptors");
+    const uint64_t dstage0 = sdesc(smem_u32(smem)), dstage1 = sdesc(smem_u32(smem + STAGE_BYTES));
+    constexpr uint64_t A_PL = TILE_A >> 4, B0 = (4 * TILE_A) >> 4, B_LO = TILE_B >> 4, B_RE = (BN * 128) >> 4;
     for (int kt = 0; kt < nk; ++kt) {
       const int s = kt % STAGES;
       const uint32_t d = tmem + (uint32_t)(2 * BN * (kt % NACC));  // [re | im] columns of pair kt % NACC
@@ -307,26 +314,23 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       }
       if (*abort_flag) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t sa = smem_u32(smem + s * STAGE_BYTES);
-      const uint32_t sb = sa + 4 * TILE_A;
+      const uint64_t ds = s ? dstage1 : dstage0;
 #pragma unroll
       for (int ks = 0; ks < BK / 8; ++ks) {
-        uint64_t a[4];
-#pragma unroll
-        for (int pl = 0; pl < 4; ++pl) a[pl] = sdesc(sa + pl * TILE_A) + (uint64_t)(ks * 2);  // +32 bytes per K=8 step
-        // [Re | Im] and [-Im | Re] windows of the hi and lo B planes
-        const uint64_t bre_hi = sdesc(sb + BN * 128) + (uint64_t)(ks * 2);
-        const uint64_t bre_lo = sdesc(sb + TILE_B + BN * 128) + (uint64_t)(ks * 2);
-        const uint64_t bim_hi = sdesc(sb) + (uint64_t)(ks * 2);
-        const uint64_t bim_lo = sdesc(sb + TILE_B) + (uint64_t)(ks * 2);
+        const uint64_t dk = ds + (uint64_t)(ks * 2);  // +32 bytes per K=8 step
+        // A planes Re_hi, Re_lo, Im_hi, Im_lo; the [Re | Im] and [-Im | Re]
+        // windows of the hi and lo B planes
+        const uint64_t a0 = dk, a1 = dk + A_PL, a2 = dk + 2 * A_PL, a3 = dk + 3 * A_PL;
+        const uint64_t bre_hi = dk + B0 + B_RE, bre_lo = dk + B0 + B_LO + B_RE;
+        const uint64_t bim_hi = dk + B0, bim_lo = dk + B0 + B_LO;
         const uint32_t first = (kt < NACC && ks == 0) ? 0u : 1u;
         // re += Are Bre - Aim Bim,  im += Are Bim + Aim Bre  (3xTF32: hi hi, hi lo, lo hi)
-        umma(d, a[0], bre_hi, IDESC, first);
-        umma(d, a[0], bre_lo, IDESC, 1);
-        umma(d, a[1], bre_hi, IDESC, 1);
-        umma(d, a[2], bim_hi, IDESC, 1);
-        umma(d, a[2], bim_lo, IDESC, 1);
-        umma(d, a[3], bim_hi, IDESC, 1);
+        umma(d, a0, bre_hi, IDESC, first);
+        umma(d, a0, bre_lo, IDESC, 1);
+        umma(d, a1, bre_hi, IDESC, 1);
+        umma(d, a2, bim_hi, IDESC, 1);
+        umma(d, a2, bim_lo, IDESC, 1);
+        umma(d, a3, bim_hi, IDESC, 1);
       }
       umma_commit(&empty[s]);  // stage s may be refilled once these MMAs retire
     }
