@@ -5,7 +5,7 @@ fraction k / min(2 chi_L, 2 chi_R, cap) of singular values the reference rank
 rule will keep.  Its prediction sizes the number of eigenpairs each gate
 computes (``ell``); if the prediction is too small the pipeline reports
 ``AGB_ERR_RANK`` and the gate is re-run with the plain full size (the plain
-form is both the fallback and the judge of the predictor's error).
+form is both the fallback and the arbiter of the predictor's error).
 
 Features (all O(1) on the host, per gate):
   0  log2(chi_L) / 10
