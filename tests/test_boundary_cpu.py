@@ -149,6 +149,12 @@ def test_new_entry_points_validate_arguments_without_a_gpu(lib):
     # asynchronous tensor-core GEMM: the device status word is required
     assert lib.agb_cgemm_tc_async(b"N", b"N", 1, 8, 8, 8, P, 8, 64, P, 8, 64, P, 8, 64,
                                   1.0, 0.0, 0.0, 0.0, P, 0, P, P) == _lib.AGB_ERR_ARG
+    # the GEMM's wait-limit hook is host state: set, restore (negative = default)
+    assert lib.agb_set_gemm_wait_limit(0) == _lib.AGB_OK
+    assert lib.agb_set_gemm_wait_limit(-1) == _lib.AGB_OK
+    # tridiagonalisation switch: modes 0 and 1 only
+    assert lib.agb_set_tridiag_stages(2) == _lib.AGB_ERR_ARG
+    assert lib.agb_set_tridiag_stages(1) == _lib.AGB_OK
     # no launch has failed in this process
     assert lib.agb_last_error() == b""
 
